@@ -1,0 +1,465 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the force-and-step path on GB300.
+
+Workload: 30,000 flexible three-site waters in a 96.5 A cubic box plus a
+solvated 500-bead chain (88,289 atoms after overlap removal), LJ cutoff 12 A
+switched from 10 A, Ewald real space (tolerance 1e-5) + PME 96^3 order 4,
+bonds/angles/dihedrals, Langevin 300 K, 1 fs, friction 1/ps.  Seeded
+synthetic coordinates (no dataset exists for this benchmark).
+
+A "step" is one MD step (one force evaluation + the FP64 update).  Each timed
+step is one CUDA-graph replay bracketed by CUDA events on the launching
+stream; a 256 MB buffer is rewritten between timed steps to flush the 129 MB
+L2 (the working set, ~25 MB, would otherwise stay L2-resident).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 runs one independent replica per GPU (torchrun; the path does not
+shard): value = all replicas' simulated time / max-over-ranks wall time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import numpy as np  # noqa: E402
+
+METRIC = "ns/day & atom-steps/s on 1 GB300 at force err <=1e-4 vs FP64; plain vs chosen"
+DT_FS = 1.0
+TEMPERATURE = 300.0
+FRICTION = 0.001          # 1/ps in 1/fs
+CUTOFF, SWITCH, GRID, ORDER, EWALD_TOL = 12.0, 10.0, 96, 4, 1e-5
+L2_FLUSH_BYTES = 256 << 20
+PEAKS = os.path.join(HERE, "MEASURED_PEAKS.json")
+PROFILE_INPUTS = os.path.join(HERE, "profiles", "roofline_inputs.json")
+FP32_PEAK_TFLOPS_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12   # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3000)
+    p.add_argument("--warmup", type=int, default=50)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--waters", type=int, default=30000)
+    p.add_argument("--box", type=float, default=96.5)
+    p.add_argument("--beads", type=int, default=500)
+    p.add_argument("--e2e-steps", type=int, default=100)
+    p.add_argument("--kernel-reps", type=int, default=200)
+    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--no-error-check", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload_name(a, n_atoms):
+    return ("water%dk_chain%d_%.1fA_%d_atoms_rc%g_sw%g_pme%d_o%d_langevin300K_1fs"
+            % (a.waters // 1000, a.beads, a.box, n_atoms, CUTOFF, SWITCH, GRID, ORDER))
+
+
+def make_system(a, seed):
+    from mdpy_gb300 import systems
+
+    return systems.chain_in_water(n_waters=a.waters, box=a.box, n_beads=a.beads, seed=seed)
+
+
+def make_ensemble(s, device):
+    from mdpy_gb300 import constraint as C
+    from mdpy_gb300.ensemble import Ensemble
+
+    ens = Ensemble(s.topology, s.pbc_matrix, device=device)
+    nb = C.NonbondedConstraint(s.parameters["nonbonded"], cutoff_radius=CUTOFF,
+                               switch_radius=SWITCH, ewald_error=EWALD_TOL)
+    pme = C.PMEConstraint(grid_size=GRID, order=ORDER, ewald_error=EWALD_TOL,
+                          real_space_cutoff=CUTOFF)
+    ens.add_constraints(nb, pme, C.CharmmBondConstraint(s.parameters["bond"]),
+                        C.CharmmAngleConstraint(s.parameters["angle"]),
+                        C.CharmmDihedralConstraint(None, float_parameters=s.dihedral_parameters))
+    ens.state.set_positions(s.positions)
+    ens.state.set_velocities(s.velocities)
+    return ens, nb.ewald_beta
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# distributed helpers (replicas; gloo on CPU in the tests)
+# --------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("MDG_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def reduce_max(value, world, device=None):
+    """Max of a float over ranks (the bench's wall-time rule)."""
+    if world == 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64,
+                     device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# --------------------------------------------------------------------------
+# CPU arm: the oracle port of the reference path, on the host cores
+# --------------------------------------------------------------------------
+def cpu_reference_sample(s, seconds):
+    """mdpy's CPU step restated by the oracle: LJ (cell list, hard cutoff 12 A)
+    + bare Coulomb over all pairs + bonds + angles + dihedrals per force
+    evaluation, three evaluations per Langevin step as mdpy's
+    LangevinIntegrator runs them (mdpy/integrator/langevin_integrator.py:51-64).
+    Times whole force evaluations on the full system until ``seconds`` pass."""
+    from oracle import oracle as O
+
+    t = s.topology
+    n = s.num_particles
+    p = s.parameters["nonbonded"]
+    lj = np.array([[p[ty][0], p[ty][1], p[ty][0], p[ty][1]] for ty in t.particle_types])
+    q = t.charges.reshape(-1)
+    types = t.particle_types
+    kb = np.array([s.parameters["bond"]["%s-%s" % (types[i], types[j])] for i, j in t.bonds])
+    ka = np.array([s.parameters["angle"]["%s-%s-%s" % (types[i], types[j], types[k])]
+                   for i, j, k in t.angles])
+    threads = O.num_threads()
+    evals, t0 = 0, time.perf_counter()
+    while True:
+        te = time.perf_counter()
+        f1, _ = O.nonbonded(s.positions, s.box, lj, q, t.bonded_particles, t.scaling_particles,
+                            CUTOFF, coulomb="none")
+        f2, _ = O.nonbonded(s.positions, s.box, np.zeros((n, 4)), q, t.bonded_particles,
+                            t.scaling_particles, CUTOFF, lj=False, coulomb="bare")
+        O.bonds(s.positions, s.box, t.bonds, kb)
+        O.angles(s.positions, s.box, t.angles, ka)
+        O.dihedrals(s.positions, s.box, t.dihedrals, s.dihedral_parameters)
+        evals += 1
+        if time.perf_counter() - t0 >= seconds or time.perf_counter() - te > seconds / 2:
+            break
+    per_eval = (time.perf_counter() - t0) / evals
+    per_step = 3.0 * per_eval
+    sps = 1.0 / per_step
+    from mdpy_gb300 import unit
+
+    return {
+        "ns_per_day": unit.ns_per_day(sps, DT_FS),
+        "atom_steps_per_s": n * sps,
+        "cores": threads,
+        "host_cores": os.cpu_count(),
+        "sample": ("%d full force evaluation(s) of the reference path (LJ cell list rc 12 A + "
+                   "bare Coulomb over all %d atom pairs + bonds/angles/dihedrals, FP64 C port, "
+                   "%d threads) on the %d-atom system; %.2f s per evaluation, x3 per Langevin "
+                   "step as mdpy runs it" % (evals, n, threads, n, per_eval)),
+    }
+
+
+# --------------------------------------------------------------------------
+# force error vs the FP64 oracle (a sample of atoms; structure factors use all)
+# --------------------------------------------------------------------------
+def force_error(s, ens, beta, n_sample=1000, seed=0):
+    from oracle import oracle as O
+
+    t = s.topology
+    n = s.num_particles
+    pos = ens.state.positions
+    ens.update()
+    f_gpu = ens.forces
+    p = s.parameters["nonbonded"]
+    lj = np.array([[p[ty][0], p[ty][1], p[ty][0], p[ty][1]] for ty in t.particle_types])
+    q = t.charges.reshape(-1)
+    rng = np.random.default_rng(seed)
+    sub = np.sort(rng.choice(n, size=min(n_sample, n), replace=False))
+    f_nb, _ = O.nonbonded(pos, s.box, lj, q, t.bonded_particles, t.scaling_particles, CUTOFF,
+                          switch=SWITCH, coulomb="ewald", beta=beta)
+    f_rec, _ = O.ewald_recip(pos, s.box, q, beta, O.ewald_kmax(s.box, beta, 1e-9), subset=sub)
+    f_ex, _ = O.ewald_exclusions(pos, s.box, q, t.bonded_particles, beta)
+    types = t.particle_types
+    kb = np.array([s.parameters["bond"]["%s-%s" % (types[i], types[j])] for i, j in t.bonds])
+    ka = np.array([s.parameters["angle"]["%s-%s-%s" % (types[i], types[j], types[k])]
+                   for i, j, k in t.angles])
+    f_b, _ = O.bonds(pos, s.box, t.bonds, kb)
+    f_a, _ = O.angles(pos, s.box, t.angles, ka)
+    f_d, _ = O.dihedrals(pos, s.box, t.dihedrals, s.dihedral_parameters)
+    ref = (f_nb + f_ex + f_b + f_a + f_d)[sub] + f_rec
+    err = float(np.sqrt(np.sum((f_gpu[sub] - ref) ** 2) / np.sum(ref ** 2)))
+    return err, len(sub)
+
+
+# --------------------------------------------------------------------------
+def run_reference_arm(a, world, rank):
+    if rank != 0:
+        return 0
+    s = make_system(a, seed=0)
+    r = cpu_reference_sample(s, a.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": r["ns_per_day"], "unit": "ns/day", "impl": "reference",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1000.0 * s.num_particles / r["atom_steps_per_s"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "atom_steps_per_s": r["atom_steps_per_s"],
+        "config": {"workload": workload_name(a, s.num_particles), "atoms": s.num_particles,
+                   "l2": "n/a (host)"},
+        "cpu_baseline": {"value": r["ns_per_day"], "unit": "ns/day", "cores": r["cores"],
+                         "kind": "port", "sample": r["sample"]},
+        "e2e": {"value": r["ns_per_day"], "unit": "ns/day", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    a = parse()
+    world, rank, local = dist_setup()
+    if a.impl == "reference":
+        return run_reference_arm(a, world, rank)
+
+    import torch
+
+    from mdpy_gb300 import _lib, unit
+    from mdpy_gb300.integrator import LangevinIntegrator
+
+    torch.cuda.set_device(local)
+    s = make_system(a, seed=rank)
+    n = s.num_particles
+    ens, beta = make_ensemble(s, local)
+    sysm = ens.system
+    stream = torch.cuda.current_stream()
+    sysm.set_stream(stream.cuda_stream)
+    integ = LangevinIntegrator(DT_FS, TEMPERATURE, FRICTION, seed=1000 + rank)
+    integ._configure(ens)
+    mask = ens.term_mask
+    sysm.set_graph_mode(_lib.GRAPH_STEP)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    # warm-up (graphs captured here)
+    sysm.integrate(max(a.warmup, 3), mask, want_energy=False)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K single-step graph replays, L2 flushed in between --
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = sysm.launch_count
+    for k in range(a.steps):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        sysm.integrate(1, mask, want_energy=False)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = sysm.launch_count - launches0
+    clk = clocks.stop()
+    ms_total = sum(st.elapsed_time(en) for st, en in zip(starts, ends))
+    ms_total = reduce_max(ms_total, world, device=torch.device("cuda", local)
+                          if world > 1 and os.environ.get("MDG_BENCH_BACKEND", "nccl") == "nccl"
+                          else None)
+    ms_step = ms_total / a.steps
+    sps_job = world * a.steps / (ms_total / 1000.0)
+    value = unit.ns_per_day(sps_job, DT_FS)
+    sysm.check_status()
+
+    # ---- per-stage timing (same flush protocol) ----------------------------
+    # single stages accumulate into the force buffer and the update stage
+    # moves atoms with it, so the state is saved here and restored after
+    x_save, v_save = sysm.get_positions(), sysm.get_velocities()
+    ens.update()
+    stats = sysm.nonbonded_stats()
+    stage_ms = {}
+    for name, stage in (("pack", _lib.STAGE_PACK), ("nonbonded", _lib.STAGE_NONBONDED),
+                        ("special", _lib.STAGE_SPECIAL), ("pme", _lib.STAGE_PME),
+                        ("bonded", _lib.STAGE_BONDED), ("integrate", _lib.STAGE_INTEGRATE),
+                        ("reorder", _lib.STAGE_REORDER)):
+        reps = a.kernel_reps if name == "nonbonded" else max(20, a.kernel_reps // 4)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(reps)]
+        for st, en in ev:
+            flush.fill_(1)
+            st.record(stream)
+            sysm.launch_stage(stage, mask)
+            en.record(stream)
+        torch.cuda.synchronize()
+        stage_ms[name] = float(np.mean([st.elapsed_time(en) for st, en in ev]))
+    sysm.set_positions(x_save)
+    sysm.set_velocities(v_save)
+    ens.update()  # a valid force buffer again
+
+    # pair-kernel roofline: algorithmic bytes = coordinates+charge (16 B) +
+    # LJ parameters (8 B) read once and three int64 force words (24 B) written
+    # once per atom, plus the cluster box and partner range (40 B per cluster)
+    n_pad = 32 * ((n + 31) // 32)
+    alg_bytes = 48 * n_pad + 40 * (n_pad // 32)
+    t_nb = stage_ms["nonbonded"] * 1e-3
+    peaks = {}
+    if os.path.exists(PEAKS):
+        with open(PEAKS) as fh:
+            peaks = json.load(fh)
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    traffic = None
+    if os.path.exists(PROFILE_INPUTS):
+        with open(PROFILE_INPUTS) as fh:
+            traffic = json.load(fh).get("nonbonded_dram_bytes_per_launch")
+    achieved = alg_bytes / t_nb / 1e9
+    pairs_in = stats["pairs_in_cutoff"]
+    flops = 60.0 * pairs_in / t_nb / 1e12
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "k_nonbonded",
+                "peak_source": peak_src, "alg_bytes_per_launch": alg_bytes,
+                "launch_ms": stage_ms["nonbonded"],
+                "fp32": {"achieved_tflops": flops, "nominal_peak_tflops": FP32_PEAK_TFLOPS_NOMINAL,
+                         "frac": flops / FP32_PEAK_TFLOPS_NOMINAL,
+                         "flops_per_pair": 60, "pairs_in_cutoff": pairs_in,
+                         "pair_evaluations": stats["pair_evaluations"]}}
+
+    # ---- end to end through the public API with pinned host buffers --------
+    x_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    v_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    sysm.get_positions_ptr(x_h.data_ptr(), _lib.HOST)
+    sysm.get_velocities_ptr(v_h.data_ptr(), _lib.HOST)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for k in range(a.e2e_steps):
+        sysm.set_positions_ptr(x_h.data_ptr(), _lib.HOST)
+        sysm.set_velocities_ptr(v_h.data_ptr(), _lib.HOST)
+        sysm.integrate(1, mask, want_energy=True)
+        sysm.get_positions_ptr(x_h.data_ptr(), _lib.HOST)
+        sysm.get_velocities_ptr(v_h.data_ptr(), _lib.HOST)
+        e_terms, ke = sysm.get_energies()
+    torch.cuda.synchronize()
+    e2e_s = reduce_max(time.perf_counter() - t0, world,
+                       device=torch.device("cuda", local)
+                       if world > 1 and os.environ.get("MDG_BENCH_BACKEND", "nccl") == "nccl"
+                       else None)
+    e2e_value = unit.ns_per_day(world * a.e2e_steps / e2e_s, DT_FS)
+    e2e = {"value": e2e_value, "unit": "ns/day", "h2d_bytes_per_step": 2 * n * 24,
+           "d2h_bytes_per_step": 2 * n * 24 + 8 * (_lib.NUM_TERMS + 1),
+           "api": "mdg_set_positions/velocities(host) + mdg_integrate(1) + "
+                  "mdg_get_positions/velocities(host) + mdg_get_energies"}
+
+    err = None
+    cpu = None
+    if rank == 0 and world == 1:
+        if not a.no_error_check:
+            err, nsub = force_error(s, ens, beta)
+        if not a.no_cpu_baseline:
+            r = cpu_reference_sample(s, a.cpu_seconds)
+            cpu = {"value": r["ns_per_day"], "unit": "ns/day", "cores": r["cores"],
+                   "kind": "port", "sample": r["sample"],
+                   "atom_steps_per_s": r["atom_steps_per_s"]}
+
+    if rank == 0:
+        plain = {"ns_per_day": value, "atom_steps_per_s": n * sps_job, "ms_per_step": ms_step}
+        line = {
+            "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": workload_name(a, n), "atoms": n, "replicas": world,
+                       "l2": "flushed between timed steps (256 MB rewrite)",
+                       "precision": "f32 pair/PME arithmetic, int64 fixed-point (2^-32) force "
+                                    "accumulation, f64 x/v/energies",
+                       "form": "plain"},
+            "atom_steps_per_s": n * sps_job,
+            "force_rel_rms_err_vs_fp64": err,
+            "plain": plain, "chosen": dict(plain, form="plain"),
+            "roofline": roofline, "stages_ms": stage_ms, "nonbonded_stats": stats,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

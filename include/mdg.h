@@ -1,0 +1,201 @@
+/*
+ * mdg.h -- C ABI of libmdg, the GB300 (sm_103a) force-and-step engine behind
+ * the mdpy constraint / ensemble / integrator API.
+ *
+ * The reference (mdpy v0.2.1) is pure Python and has no FFI; each entry point
+ * below names the reference interface whose work it takes over (paths are
+ * relative to the mdpy source tree).  The Python host layer in
+ * mdpy_gb300/ binds these through ctypes.
+ *
+ * Conventions
+ *  - Every function returns an int status: MDG_OK (0) or an MDG_ERR_* code.
+ *    mdg_last_error() returns a message for the calling thread's last error.
+ *  - Units are mdpy's: Angstrom, Dalton, femtosecond, elementary charge,
+ *    energy Da*A^2/fs^2 (mdpy/unit/__init__.py:31-49).
+ *  - Boxes are orthorhombic (the diagonal of mdpy's pbc_matrix); a
+ *    non-diagonal pbc_matrix is rejected with MDG_ERR_BOX.
+ *  - Arrays are row-major.  Host pointers are read/written synchronously
+ *    unless a function says `where`; with where == MDG_DEVICE the pointer is a
+ *    device address (e.g. a torch tensor's data_ptr()) in the system's device.
+ *  - The library owns all device memory of a system; nothing is kept from a
+ *    caller's pointer after the call returns.
+ *  - Calls on one system are not thread-safe; use one system per thread.
+ *  - Work is issued on the system's stream (mdg_system_set_stream).
+ */
+#ifndef MDG_H
+#define MDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDG_API __attribute__((visibility("default")))
+
+/* status codes */
+#define MDG_OK 0
+#define MDG_ERR_INVALID 1       /* bad argument or call order */
+#define MDG_ERR_CUDA 2          /* CUDA runtime failure */
+#define MDG_ERR_NOMEM 3         /* device allocation failed */
+#define MDG_ERR_BOX 4           /* box not orthorhombic / not positive */
+#define MDG_ERR_CUTOFF 5        /* cutoff >= half the box (minimum image breaks) */
+#define MDG_ERR_PARTICLE_LOSS 6 /* non-finite position or velocity */
+#define MDG_ERR_OVERFLOW 7      /* fixed-point force/energy overflow */
+#define MDG_ERR_CUFFT 8         /* cuFFT failure */
+#define MDG_ERR_TIMEOUT 9       /* a bounded device wait gave up */
+#define MDG_ERR_CAPACITY 10     /* caller buffer too small */
+#define MDG_ERR_STATE 11        /* operation needs state that is not set */
+
+/* memory location of a caller pointer */
+#define MDG_HOST 0
+#define MDG_DEVICE 1
+
+/* force / energy terms (bit masks and energy slots) */
+#define MDG_TERM_LJ 0          /* Lennard-Jones (incl. 1-4 pairs)            */
+#define MDG_TERM_COUL_REAL 1   /* Ewald real space erfc, or bare Coulomb     */
+#define MDG_TERM_COUL_RECIP 2  /* PME reciprocal + self + net-charge + excl. */
+#define MDG_TERM_BOND 3
+#define MDG_TERM_ANGLE 4
+#define MDG_TERM_DIHEDRAL 5
+#define MDG_TERM_IMPROPER 6
+#define MDG_NUM_TERMS 7
+#define MDG_MASK(t) (1u << (t))
+#define MDG_MASK_ALL ((1u << MDG_NUM_TERMS) - 1u)
+
+/* Coulomb modes of the short-range constraint */
+#define MDG_COUL_NONE 0
+#define MDG_COUL_EWALD 1 /* erfc(beta r)/r inside the cutoff            */
+#define MDG_COUL_BARE 2  /* 1/r, all pairs, minimum image, no cutoff   */
+
+/* integrators */
+#define MDG_INTEGRATOR_VERLET 0
+#define MDG_INTEGRATOR_LANGEVIN 1
+
+typedef struct mdg_system mdg_system;
+
+/* ---- diagnostics -------------------------------------------------------- */
+MDG_API int mdg_version(int *major, int *minor);
+MDG_API const char *mdg_last_error(void);
+
+/* ---- system lifetime ---------------------------------------------------- */
+/* Replaces the device state the reference rebuilds per call
+ * (Ensemble.__init__ + State, mdpy/ensemble.py:16-31, mdpy/core/state.py:19-28):
+ * allocates a system of n_atoms on `device` with box edges box[3]. */
+MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_system **out);
+MDG_API int mdg_system_destroy(mdg_system *sys);
+/* cudaStream_t passed as void*; NULL restores the system's own stream */
+MDG_API int mdg_system_set_stream(mdg_system *sys, void *stream);
+/* State.set_pbc_matrix (mdpy/core/state.py:47-54), diagonal only */
+MDG_API int mdg_system_set_box(mdg_system *sys, const double *box);
+
+/* ---- static parameters (bind_ensemble work) ----------------------------- */
+/* Topology.join masses/charges (mdpy/core/topology.py:59-70) */
+MDG_API int mdg_set_masses(mdg_system *sys, const double *masses);
+MDG_API int mdg_set_charges(mdg_system *sys, const double *charges);
+/* CharmmNonbondedConstraint.bind_ensemble per-atom [eps, sigma, eps14, sigma14]
+ * (mdpy/constraint/charmm_nonbonded_constraint.py:48-62), shape (n, 4) */
+MDG_API int mdg_set_lj(mdg_system *sys, const double *params);
+/* Topology.bonded_particles (1-2/1-3, excluded) and scaling_particles (1-4)
+ * as dense -1 padded (n, width) arrays (mdpy/core/topology.py:71-79) */
+MDG_API int mdg_set_exclusions(mdg_system *sys, const int32_t *bonded, int bonded_width,
+                               const int32_t *scaling, int scaling_width);
+
+/* ---- nonbonded configuration ------------------------------------------- */
+/* CharmmNonbondedConstraint(cutoff_radius) + ElectrostaticConstraint, re-designed:
+ * LJ on/off, optional CHARMM switch from `switch_radius` (<= 0: hard cutoff as
+ * the reference), Coulomb mode MDG_COUL_*, Ewald splitting `beta` (1/A). */
+MDG_API int mdg_nonbonded_config(mdg_system *sys, double cutoff, double switch_radius,
+                                 int lj_on, int coulomb_mode, double beta);
+/* PME reciprocal space (no reference counterpart; LONG_RANGE_SOLVER names it,
+ * mdpy/constraint/__init__.py:22): grid K[3], B-spline order, splitting beta. */
+MDG_API int mdg_pme_config(mdg_system *sys, const int *grid, int order, double beta);
+/* spatial re-sort interval (steps) of the atom clusters; default 20 */
+MDG_API int mdg_set_reorder_interval(mdg_system *sys, int steps);
+
+/* ---- bonded terms (CharmmBond/Angle/Dihedral/ImproperConstraint.bind_ensemble) */
+/* bonds: idx (n,2), prm (n,2) = (k, r0)          charmm_bond_constraint.py:32-50
+ * angles: idx (n,3), prm (n,4) = (k, th0, ku, u0) charmm_angle_constraint.py:116-136
+ * dihedrals: idx (n,4), prm (n,3) = (k, n, delta) charmm_dihedral_constraint.py:33-56
+ * impropers: idx (n,4), prm (n,2) = (k, psi0)     charmm_improper_constraint.py  */
+MDG_API int mdg_set_bonds(mdg_system *sys, int n, const int32_t *idx, const double *prm);
+MDG_API int mdg_set_angles(mdg_system *sys, int n, const int32_t *idx, const double *prm);
+MDG_API int mdg_set_dihedrals(mdg_system *sys, int n, const int32_t *idx, const double *prm);
+MDG_API int mdg_set_impropers(mdg_system *sys, int n, const int32_t *idx, const double *prm);
+
+/* ---- state ------------------------------------------------------------- */
+/* State.set_positions / set_velocities (mdpy/core/state.py:56-65), (n,3) FP64 */
+MDG_API int mdg_set_positions(mdg_system *sys, const double *x, int where);
+MDG_API int mdg_set_velocities(mdg_system *sys, const double *v, int where);
+/* positions wrapped into [-L/2, L/2) as wrap_positions (mdpy/utils/pbc.py:28-36) */
+MDG_API int mdg_get_positions(mdg_system *sys, double *x, int where);
+MDG_API int mdg_get_velocities(mdg_system *sys, double *v, int where);
+
+/* ---- forces and energies ----------------------------------------------- */
+/* Ensemble.update / Constraint.update (mdpy/ensemble.py:53-61): evaluate the
+ * terms in `mask` into the system force buffer (int64 fixed point, 2^-32)
+ * and their energies. */
+MDG_API int mdg_compute_forces(mdg_system *sys, unsigned mask);
+/* Ensemble.forces / Constraint.forces: (n,3) FP64 in atom order */
+MDG_API int mdg_get_forces(mdg_system *sys, double *f, int where);
+/* energies[MDG_NUM_TERMS] of the last evaluation (reciprocal slot includes the
+ * self, net-charge and exclusion terms) and the kinetic energy */
+MDG_API int mdg_get_energies(mdg_system *sys, double *energies, double *kinetic);
+/* Ensemble._update_kinetic_energy (mdpy/ensemble.py:63-71), FP64 */
+MDG_API int mdg_kinetic_energy(mdg_system *sys, double *kinetic);
+
+/* ---- integration ------------------------------------------------------- */
+/* VerletIntegrator / LangevinIntegrator (mdpy/integrator/*.py) re-designed:
+ * velocity Verlet or Groenbech-Jensen--Farago Langevin, FP64 x/v, one force
+ * evaluation per step, Philox4x32-10 noise keyed by (seed, atom, step). */
+MDG_API int mdg_integrator_config(mdg_system *sys, int kind, double dt, double temperature,
+                                  double friction, uint64_t seed);
+/* Integrator.integrate(ensemble, num_steps) (mdpy/integrator/integrator.py:24-27):
+ * advances n_steps over the force terms in `mask`; energies of the final
+ * step are evaluated when want_energy != 0.  Steps run as CUDA graphs. */
+MDG_API int mdg_integrate(mdg_system *sys, int n_steps, unsigned mask, int want_energy);
+/* current step counter (the Philox counter of the next step) */
+MDG_API int mdg_get_step(mdg_system *sys, uint64_t *step);
+MDG_API int mdg_set_step(mdg_system *sys, uint64_t step);
+
+/* ---- parity / diagnostics ---------------------------------------------- */
+/* All unordered pairs (atom indices i<j, int32 pairs) that the short-range
+ * kernel evaluates with r <= cutoff, from the same kernel code path as the
+ * forces.  *count receives the total; at most `capacity` pairs are written. */
+MDG_API int mdg_pairset_dump(mdg_system *sys, int32_t *pairs, int64_t capacity,
+                             int64_t *count);
+/* thermostat noise of step `step`, (n,3) float32 (same Philox stream as the
+ * Langevin kernel) */
+MDG_API int mdg_langevin_noise(mdg_system *sys, uint64_t step, float *out);
+/* device-side status word: 0 or MDG_ERR_* raised by a kernel since the last call */
+MDG_API int mdg_check_status(mdg_system *sys);
+/* statistics of the last nonbonded evaluation: [0] pair evaluations issued,
+ * [1] pairs inside the cutoff, [2] cluster candidates, [3] clusters */
+MDG_API int mdg_nonbonded_stats(mdg_system *sys, int64_t *stats);
+/* number of kernels libmdg has launched on this system so far */
+MDG_API int mdg_launch_count(mdg_system *sys, int64_t *count);
+
+/* graph granularity of mdg_integrate: MDG_GRAPH_CHUNK (default) replays
+ * `reorder_interval` steps per graph launch; MDG_GRAPH_STEP replays one graph
+ * per MD step (so a caller can bracket single steps with events). */
+#define MDG_GRAPH_CHUNK 0
+#define MDG_GRAPH_STEP 1
+MDG_API int mdg_set_graph_mode(mdg_system *sys, int mode);
+
+/* Launch one stage of a force evaluation on the system stream, for timing and
+ * profiling (the state must have been evaluated once).  Stages that
+ * accumulate forces leave the force buffer invalid. */
+#define MDG_STAGE_PACK 0
+#define MDG_STAGE_NONBONDED 1
+#define MDG_STAGE_SPECIAL 2
+#define MDG_STAGE_PME 3
+#define MDG_STAGE_BONDED 4
+#define MDG_STAGE_REORDER 5
+#define MDG_STAGE_INTEGRATE 6 /* pre + post update kernels */
+MDG_API int mdg_launch_stage(mdg_system *sys, int stage, unsigned mask);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDG_H */

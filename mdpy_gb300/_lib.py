@@ -1,0 +1,322 @@
+"""ctypes binding of libmdg (include/mdg.h).
+
+``System`` owns one ``mdg_system``.  Every call checks the returned status
+and raises the mdpy-style exception of :mod:`mdpy_gb300.error`.  The shared
+library is built in-tree (``python -m mdpy_gb300.build``); if it is missing
+the import of this module fails loudly -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .error import status_to_exception
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmdg.so")
+
+# constants mirrored from include/mdg.h
+HOST, DEVICE = 0, 1
+TERM_LJ, TERM_COUL_REAL, TERM_COUL_RECIP, TERM_BOND, TERM_ANGLE, TERM_DIHEDRAL, TERM_IMPROPER = range(7)
+NUM_TERMS = 7
+TERM_NAMES = ("lj", "coulomb_real", "coulomb_recip", "bond", "angle", "dihedral", "improper")
+COUL_NONE, COUL_EWALD, COUL_BARE = 0, 1, 2
+INTEGRATOR_VERLET, INTEGRATOR_LANGEVIN = 0, 1
+MASK_ALL = (1 << NUM_TERMS) - 1
+
+
+def mask(*terms):
+    m = 0
+    for t in terms:
+        m |= 1 << t
+    return m
+
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_c_dbl_p = ctypes.POINTER(ctypes.c_double)
+_c_i32_p = ctypes.POINTER(ctypes.c_int32)
+_c_i64_p = ctypes.POINTER(ctypes.c_int64)
+_c_f32_p = ctypes.POINTER(ctypes.c_float)
+_c_u64_p = ctypes.POINTER(ctypes.c_uint64)
+_sys_p = ctypes.c_void_p
+
+# name -> argtypes (every function returns int)
+SIGNATURES = {
+    "mdg_version": [_c_int_p, _c_int_p],
+    "mdg_system_create": [ctypes.c_int, ctypes.c_int, _c_dbl_p, ctypes.POINTER(_sys_p)],
+    "mdg_system_destroy": [_sys_p],
+    "mdg_system_set_stream": [_sys_p, ctypes.c_void_p],
+    "mdg_system_set_box": [_sys_p, _c_dbl_p],
+    "mdg_set_masses": [_sys_p, _c_dbl_p],
+    "mdg_set_charges": [_sys_p, _c_dbl_p],
+    "mdg_set_lj": [_sys_p, _c_dbl_p],
+    "mdg_set_exclusions": [_sys_p, _c_i32_p, ctypes.c_int, _c_i32_p, ctypes.c_int],
+    "mdg_nonbonded_config": [_sys_p, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                             ctypes.c_double],
+    "mdg_pme_config": [_sys_p, _c_int_p, ctypes.c_int, ctypes.c_double],
+    "mdg_set_reorder_interval": [_sys_p, ctypes.c_int],
+    "mdg_set_bonds": [_sys_p, ctypes.c_int, _c_i32_p, _c_dbl_p],
+    "mdg_set_angles": [_sys_p, ctypes.c_int, _c_i32_p, _c_dbl_p],
+    "mdg_set_dihedrals": [_sys_p, ctypes.c_int, _c_i32_p, _c_dbl_p],
+    "mdg_set_impropers": [_sys_p, ctypes.c_int, _c_i32_p, _c_dbl_p],
+    "mdg_set_positions": [_sys_p, ctypes.c_void_p, ctypes.c_int],
+    "mdg_set_velocities": [_sys_p, ctypes.c_void_p, ctypes.c_int],
+    "mdg_get_positions": [_sys_p, ctypes.c_void_p, ctypes.c_int],
+    "mdg_get_velocities": [_sys_p, ctypes.c_void_p, ctypes.c_int],
+    "mdg_compute_forces": [_sys_p, ctypes.c_uint],
+    "mdg_get_forces": [_sys_p, ctypes.c_void_p, ctypes.c_int],
+    "mdg_get_energies": [_sys_p, _c_dbl_p, _c_dbl_p],
+    "mdg_kinetic_energy": [_sys_p, _c_dbl_p],
+    "mdg_integrator_config": [_sys_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                              ctypes.c_double, ctypes.c_uint64],
+    "mdg_integrate": [_sys_p, ctypes.c_int, ctypes.c_uint, ctypes.c_int],
+    "mdg_get_step": [_sys_p, _c_u64_p],
+    "mdg_set_step": [_sys_p, ctypes.c_uint64],
+    "mdg_pairset_dump": [_sys_p, _c_i32_p, ctypes.c_int64, _c_i64_p],
+    "mdg_langevin_noise": [_sys_p, ctypes.c_uint64, _c_f32_p],
+    "mdg_check_status": [_sys_p],
+    "mdg_nonbonded_stats": [_sys_p, _c_i64_p],
+    "mdg_launch_count": [_sys_p, _c_i64_p],
+    "mdg_set_graph_mode": [_sys_p, ctypes.c_int],
+    "mdg_launch_stage": [_sys_p, ctypes.c_int, ctypes.c_uint],
+}
+
+GRAPH_CHUNK, GRAPH_STEP = 0, 1
+STAGE_PACK, STAGE_NONBONDED, STAGE_SPECIAL, STAGE_PME, STAGE_BONDED, STAGE_REORDER, \
+    STAGE_INTEGRATE = range(7)
+
+_lib = None
+
+
+def load():
+    """Load libmdg.so; raises ImportError when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libmdg.so not found at %s; build it with `python -m mdpy_gb300.build` "
+                          "(this package has no CPU fallback)" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, argtypes in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = ctypes.c_int
+    lib.mdg_last_error.argtypes = []
+    lib.mdg_last_error.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().mdg_last_error().decode("utf-8", "replace")
+        raise status_to_exception(rc, msg)
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != tuple(shape):
+        a = a.reshape(shape)
+    return a
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_c_dbl_p)
+
+
+class System:
+    """One device-resident MD system (``mdg_system``)."""
+
+    def __init__(self, n_atoms, box, device=0):
+        self._lib = load()
+        self.n = int(n_atoms)
+        self.device = int(device)
+        box = _f64(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+        h = _sys_p()
+        check(self._lib.mdg_system_create(self.device, self.n, _dp(box), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mdg_system_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- configuration ----------------------------------------------------
+    def set_stream(self, stream_ptr):
+        check(self._lib.mdg_system_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def set_box(self, box):
+        box = _f64(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+        check(self._lib.mdg_system_set_box(self._h, _dp(box)))
+
+    def set_masses(self, m):
+        m = _f64(m).reshape(-1)
+        check(self._lib.mdg_set_masses(self._h, _dp(m)))
+
+    def set_charges(self, q):
+        q = _f64(q).reshape(-1)
+        check(self._lib.mdg_set_charges(self._h, _dp(q)))
+
+    def set_lj(self, params):
+        p = _f64(params).reshape(self.n, 4)
+        check(self._lib.mdg_set_lj(self._h, _dp(p)))
+
+    def set_exclusions(self, bonded, scaling):
+        b = _i32(np.asarray(bonded).reshape(self.n, -1))
+        s = _i32(np.asarray(scaling).reshape(self.n, -1))
+        check(self._lib.mdg_set_exclusions(self._h, b.ctypes.data_as(_c_i32_p), b.shape[1],
+                                           s.ctypes.data_as(_c_i32_p), s.shape[1]))
+
+    def nonbonded_config(self, cutoff, switch_radius=0.0, lj=True, coulomb=COUL_NONE, beta=0.0):
+        check(self._lib.mdg_nonbonded_config(self._h, float(cutoff), float(switch_radius or 0.0),
+                                             int(bool(lj)), int(coulomb), float(beta)))
+
+    def pme_config(self, grid, order, beta):
+        g = (ctypes.c_int * 3)(*[int(k) for k in np.broadcast_to(np.asarray(grid), (3,))])
+        check(self._lib.mdg_pme_config(self._h, g, int(order), float(beta)))
+
+    def set_reorder_interval(self, steps):
+        check(self._lib.mdg_set_reorder_interval(self._h, int(steps)))
+
+    def _terms(self, fn, idx, prm, wi, wp):
+        idx = _i32(np.asarray(idx).reshape(-1, wi))
+        prm = _f64(np.asarray(prm, dtype=np.float64).reshape(-1, wp))
+        if idx.shape[0] != prm.shape[0]:
+            raise ValueError("index and parameter rows differ")
+        check(fn(self._h, idx.shape[0], idx.ctypes.data_as(_c_i32_p), _dp(prm)))
+
+    def set_bonds(self, idx, prm):
+        self._terms(self._lib.mdg_set_bonds, idx, prm, 2, 2)
+
+    def set_angles(self, idx, prm):
+        self._terms(self._lib.mdg_set_angles, idx, prm, 3, 4)
+
+    def set_dihedrals(self, idx, prm):
+        self._terms(self._lib.mdg_set_dihedrals, idx, prm, 4, 3)
+
+    def set_impropers(self, idx, prm):
+        self._terms(self._lib.mdg_set_impropers, idx, prm, 4, 2)
+
+    def integrator_config(self, kind, dt, temperature=0.0, friction=0.0, seed=0):
+        check(self._lib.mdg_integrator_config(self._h, int(kind), float(dt), float(temperature),
+                                              float(friction), ctypes.c_uint64(int(seed))))
+
+    # -- state ------------------------------------------------------------
+    def set_positions(self, x):
+        x = _f64(x).reshape(self.n, 3)
+        check(self._lib.mdg_set_positions(self._h, x.ctypes.data, HOST))
+
+    def set_positions_ptr(self, ptr, where=DEVICE):
+        check(self._lib.mdg_set_positions(self._h, ctypes.c_void_p(ptr), int(where)))
+
+    def set_velocities(self, v):
+        v = _f64(v).reshape(self.n, 3)
+        check(self._lib.mdg_set_velocities(self._h, v.ctypes.data, HOST))
+
+    def set_velocities_ptr(self, ptr, where=DEVICE):
+        check(self._lib.mdg_set_velocities(self._h, ctypes.c_void_p(ptr), int(where)))
+
+    def get_positions(self, out=None):
+        out = np.empty((self.n, 3)) if out is None else out
+        check(self._lib.mdg_get_positions(self._h, out.ctypes.data, HOST))
+        return out
+
+    def get_positions_ptr(self, ptr, where=DEVICE):
+        check(self._lib.mdg_get_positions(self._h, ctypes.c_void_p(ptr), int(where)))
+
+    def get_velocities(self, out=None):
+        out = np.empty((self.n, 3)) if out is None else out
+        check(self._lib.mdg_get_velocities(self._h, out.ctypes.data, HOST))
+        return out
+
+    def get_velocities_ptr(self, ptr, where=DEVICE):
+        check(self._lib.mdg_get_velocities(self._h, ctypes.c_void_p(ptr), int(where)))
+
+    # -- forces / energies -------------------------------------------------
+    def compute_forces(self, term_mask=MASK_ALL):
+        check(self._lib.mdg_compute_forces(self._h, int(term_mask)))
+
+    def get_forces(self, out=None):
+        out = np.empty((self.n, 3)) if out is None else out
+        check(self._lib.mdg_get_forces(self._h, out.ctypes.data, HOST))
+        return out
+
+    def get_energies(self):
+        e = np.zeros(NUM_TERMS)
+        ke = ctypes.c_double(0.0)
+        check(self._lib.mdg_get_energies(self._h, _dp(e), ctypes.byref(ke)))
+        return e, ke.value
+
+    def kinetic_energy(self):
+        ke = ctypes.c_double(0.0)
+        check(self._lib.mdg_kinetic_energy(self._h, ctypes.byref(ke)))
+        return ke.value
+
+    def integrate(self, n_steps, term_mask=MASK_ALL, want_energy=True):
+        check(self._lib.mdg_integrate(self._h, int(n_steps), int(term_mask), int(bool(want_energy))))
+
+    @property
+    def step(self):
+        v = ctypes.c_uint64(0)
+        check(self._lib.mdg_get_step(self._h, ctypes.byref(v)))
+        return v.value
+
+    @step.setter
+    def step(self, value):
+        check(self._lib.mdg_set_step(self._h, ctypes.c_uint64(int(value))))
+
+    # -- diagnostics --------------------------------------------------------
+    def pairset(self, capacity=None):
+        cap = int(capacity) if capacity is not None else max(1 << 20, self.n * 800)
+        while True:
+            buf = np.empty((cap, 2), dtype=np.int32)
+            cnt = ctypes.c_int64(0)
+            rc = self._lib.mdg_pairset_dump(self._h, buf.ctypes.data_as(_c_i32_p), cap,
+                                            ctypes.byref(cnt))
+            if rc == 10 and cnt.value > cap:   # MDG_ERR_CAPACITY
+                cap = int(cnt.value)
+                continue
+            check(rc)
+            return buf[:cnt.value]
+
+    def langevin_noise(self, step):
+        out = np.empty((self.n, 3), dtype=np.float32)
+        check(self._lib.mdg_langevin_noise(self._h, ctypes.c_uint64(int(step)),
+                                           out.ctypes.data_as(_c_f32_p)))
+        return out
+
+    def check_status(self):
+        check(self._lib.mdg_check_status(self._h))
+
+    def nonbonded_stats(self):
+        v = np.zeros(4, dtype=np.int64)
+        check(self._lib.mdg_nonbonded_stats(self._h, v.ctypes.data_as(_c_i64_p)))
+        return {"pair_evaluations": int(v[0]), "pairs_in_cutoff": int(v[1]),
+                "cluster_candidates": int(v[2]), "clusters": int(v[3])}
+
+    def set_graph_mode(self, mode):
+        check(self._lib.mdg_set_graph_mode(self._h, int(mode)))
+
+    def launch_stage(self, stage, term_mask=MASK_ALL):
+        check(self._lib.mdg_launch_stage(self._h, int(stage), int(term_mask)))
+
+    @property
+    def launch_count(self):
+        v = ctypes.c_int64(0)
+        check(self._lib.mdg_launch_count(self._h, ctypes.byref(v)))
+        return v.value

@@ -1,0 +1,986 @@
+// mdg_api.cu -- the extern "C" entry points of libmdg (declared in include/mdg.h)
+// and the orchestration of one force evaluation / MD step.
+//
+// One force evaluation (Ensemble.update, mdpy/ensemble.py:53-61):
+//   [reorder]  spatial re-sort (every reorder_interval steps)
+//   pack       FP32 cluster coordinates, bounding boxes, zeroed force slots
+//   nonbonded  LJ + Ewald real space (or LJ + bare Coulomb), half shell
+//   special    1-4 pairs and the Ewald exclusion correction
+//   pme        spread -> R2C -> convolve -> C2R -> gather
+//   bonded     bonds, angles, dihedrals, impropers
+// One MD step (Integrator.integrate, one step): pre-force update, force
+// evaluation, post-force update.  mdg_integrate replays chunks of
+// `reorder_interval` steps as one CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mdg_internal.cuh"
+
+using namespace mdg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where) {
+    return fail(e == cudaErrorMemoryAllocation ? MDG_ERR_NOMEM : MDG_ERR_CUDA, "%s: %s", where,
+                cudaGetErrorString(e));
+}
+
+#define CK(call, where)                                   \
+    do {                                                  \
+        cudaError_t _e = (call);                          \
+        if (_e != cudaSuccess) return cuda_fail(_e, where); \
+    } while (0)
+
+template <typename T>
+int dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    return MDG_OK;
+}
+
+template <typename T>
+void dfree(T *&p) {
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+int check_sys(mdg_system *s) {
+    if (!s) return fail(MDG_ERR_INVALID, "null system");
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return MDG_OK;
+}
+
+void drop_one(Graph &g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+    g.steps = 0;
+}
+
+void drop_graph(mdg_system *s) {
+    drop_one(s->graph);
+    drop_one(s->graph_step[0]);
+    drop_one(s->graph_step[1]);
+}
+
+int validate_box(const double *box, double cutoff) {
+    for (int d = 0; d < 3; ++d) {
+        if (!(box[d] > 0) || !std::isfinite(box[d]))
+            return fail(MDG_ERR_BOX, "box edge %d is %g; edges must be positive", d, box[d]);
+        if (cutoff > 0 && !(cutoff < 0.5 * box[d]))
+            return fail(MDG_ERR_CUTOFF,
+                        "cutoff %g must be below half the box edge %g (minimum image)", cutoff,
+                        box[d]);
+    }
+    return MDG_OK;
+}
+
+int read_status(mdg_system *s) {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+       "status read");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    if (st) {
+        CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
+        for (int code = 1; code < 31; ++code)
+            if (st & (1 << code)) {
+                switch (code) {
+                    case MDG_ERR_PARTICLE_LOSS:
+                        return fail(code, "non-finite position or velocity");
+                    case MDG_ERR_OVERFLOW:
+                        return fail(code, "force or energy beyond the int64 fixed-point range");
+                    default:
+                        return fail(code, "device status %d", code);
+                }
+            }
+    }
+    return MDG_OK;
+}
+
+int evaluate(mdg_system *s, unsigned mask, int energy) {
+    if (s->need_reorder) {
+        CK(launch_reorder(s), "reorder");
+        s->need_reorder = 0;
+        s->steps_since_reorder = 0;
+    }
+    if (energy) {
+        CK(cudaMemsetAsync(s->energy, 0, sizeof(long long) * kEnergySlots, s->stream), "memset");
+        CK(cudaMemsetAsync(s->stats, 0, sizeof(unsigned long long) * 4, s->stream), "memset");
+    }
+    CK(launch_pack(s), "pack");
+    CK(launch_nonbonded(s, mask, energy, 0), "nonbonded");
+    CK(launch_special(s, mask, energy, 0), "special pairs");
+    if ((mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on) {
+        int cr = 0;
+        cudaError_t e = launch_pme(s, energy, &cr);
+        if (cr != CUFFT_SUCCESS) return fail(MDG_ERR_CUFFT, "cuFFT execution failed (%d)", cr);
+        CK(e, "pme");
+    }
+    CK(launch_bonded(s, mask, energy), "bonded");
+    return MDG_OK;
+}
+
+int md_step(mdg_system *s, unsigned mask, int energy) {
+    CK(launch_integrate_pre(s), "integrate pre");
+    if (s->steps_since_reorder >= s->reorder_interval) s->need_reorder = 1;
+    int rc = evaluate(s, mask, energy);
+    if (rc) return rc;
+    CK(launch_integrate_post(s, energy), "integrate post");
+    s->steps_since_reorder += 1;
+    s->step += 1;
+    return MDG_OK;
+}
+
+// Capture `nsteps` MD steps (the first re-sorting the atoms when `resort`)
+// into g; host-side counters are restored, the launch count per replay is
+// kept in g.steps.
+int capture_steps(mdg_system *s, Graph &g, int nsteps, int resort, unsigned mask) {
+    const long long saved = s->launches;
+    const int saved_since = s->steps_since_reorder, saved_need = s->need_reorder;
+    const uint64_t saved_step = s->step;
+    s->need_reorder = resort ? 1 : 0;
+    if (!resort) s->steps_since_reorder = 0;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture");
+    int crc = MDG_OK;
+    for (int k = 0; k < nsteps && !crc; ++k) crc = md_step(s, mask, 0);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
+    s->steps_since_reorder = saved_since;
+    s->need_reorder = saved_need;
+    s->step = saved_step;
+    const long long per = s->launches - saved;
+    s->launches = saved;
+    if (crc) {
+        if (graph) cudaGraphDestroy(graph);
+        return crc;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "end capture");
+    ce = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+        g.exec = nullptr;
+        return cuda_fail(ce, "graph instantiate");
+    }
+    g.steps = (int)per;
+    g.mask = mask;
+    return MDG_OK;
+}
+
+int ready_for_forces(mdg_system *s, unsigned mask) {
+    if (!s->have_x) return fail(MDG_ERR_STATE, "positions have not been set");
+    if ((mask & (MDG_MASK(MDG_TERM_LJ) | MDG_MASK(MDG_TERM_COUL_REAL))) && !s->nb_configured)
+        return fail(MDG_ERR_STATE, "nonbonded terms requested but not configured");
+    if ((mask & MDG_MASK(MDG_TERM_LJ)) && s->lj_on && !s->have_lj)
+        return fail(MDG_ERR_STATE, "LJ parameters have not been set");
+    if ((mask & (MDG_MASK(MDG_TERM_COUL_REAL) | MDG_MASK(MDG_TERM_COUL_RECIP))) &&
+        !s->have_charges)
+        return fail(MDG_ERR_STATE, "charges have not been set");
+    return MDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+MDG_API int mdg_version(int *major, int *minor) {
+    if (major) *major = 1;
+    if (minor) *minor = 0;
+    return MDG_OK;
+}
+
+MDG_API const char *mdg_last_error(void) { return g_last_error.c_str(); }
+
+MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_system **out) {
+    if (!out) return fail(MDG_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (n_atoms <= 0 || n_atoms > (1 << 26)) return fail(MDG_ERR_INVALID, "n_atoms %d out of range", n_atoms);
+    if (!box) return fail(MDG_ERR_INVALID, "box is null");
+    int rc = validate_box(box, 0.0);
+    if (rc) return rc;
+    CK(cudaSetDevice(device), "cudaSetDevice");
+    mdg_system *s = new mdg_system();
+    s->device = device;
+    s->n = n_atoms;
+    s->n_pad = (n_atoms + kCluster - 1) / kCluster * kCluster;
+    s->n_clusters = s->n_pad / kCluster;
+    for (int d = 0; d < 3; ++d) s->box[d] = box[d];
+    cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    s->stream = s->own_stream;
+    const int n = s->n, np = s->n_pad;
+#define AL(ptr, cnt)                     \
+    if ((rc = dalloc(&(ptr), (cnt)))) { \
+        mdg_system_destroy(s);          \
+        return rc;                      \
+    }
+    AL(s->mass, n);
+    AL(s->inv_mass, n);
+    AL(s->charge, n);
+    AL(s->lj, n);
+    AL(s->perm, np);
+    AL(s->inv_perm, n);
+    AL(s->q_sorted, np);
+    AL(s->prm_sorted, np);
+    AL(s->cluster_partner_range, s->n_clusters);
+    AL(s->atom_key, n);
+    AL(s->tmp_perm, n);
+    AL(s->x, 3 * (size_t)n);
+    AL(s->v, 3 * (size_t)n);
+    AL(s->f, 3 * (size_t)np);
+    AL(s->xq, np);
+    AL(s->bbox, 2 * (size_t)s->n_clusters);
+    AL(s->energy, kEnergySlots);
+    AL(s->status, 1);
+    AL(s->stats, 4);
+    AL(s->step_dev, 1);
+    AL(s->fout, 3 * (size_t)n);
+    AL(s->dump_count, 1);
+    AL(s->partners, 1);
+    AL(s->partners_sorted, 1);
+#undef AL
+    cudaMemset(s->energy, 0, sizeof(long long) * kEnergySlots);
+    cudaMemset(s->status, 0, sizeof(int));
+    cudaMemset(s->step_dev, 0, sizeof(unsigned long long));
+    cudaMemset(s->v, 0, sizeof(double) * 3 * n);
+    cudaMemset(s->f, 0, sizeof(unsigned long long) * 3 * np);
+    cudaMemset(s->lj, 0, sizeof(float4) * n);
+    cudaMemset(s->charge, 0, sizeof(float) * n);
+    // masses default to 1 (inv 1) so kinetic terms are defined before set_masses
+    std::vector<double> ones(n, 1.0);
+    cudaMemcpy(s->mass, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->inv_mass, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    s->pw = 0;
+    rc = prepare_sort_grid(s);
+    if (rc) {
+        mdg_system_destroy(s);
+        return fail(rc, "sort grid allocation failed");
+    }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        mdg_system_destroy(s);
+        return cuda_fail(e, "system create");
+    }
+    *out = s;
+    return MDG_OK;
+}
+
+MDG_API int mdg_system_destroy(mdg_system *s) {
+    if (!s) return MDG_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    drop_graph(s);
+    pme_free(s);
+    dfree(s->mass);
+    dfree(s->inv_mass);
+    dfree(s->charge);
+    dfree(s->lj);
+    dfree(s->partners);
+    dfree(s->excl_pairs);
+    dfree(s->pairs14);
+    dfree(s->perm);
+    dfree(s->inv_perm);
+    dfree(s->q_sorted);
+    dfree(s->prm_sorted);
+    dfree(s->partners_sorted);
+    dfree(s->cluster_partner_range);
+    dfree(s->cell_rank);
+    dfree(s->cell_count);
+    dfree(s->cell_start);
+    dfree(s->cell_cursor);
+    dfree(s->atom_key);
+    dfree(s->tmp_perm);
+    dfree(s->scan_blocks);
+    dfree(s->x);
+    dfree(s->v);
+    dfree(s->f);
+    dfree(s->xq);
+    dfree(s->bbox);
+    dfree(s->energy);
+    dfree(s->status);
+    dfree(s->stats);
+    dfree(s->step_dev);
+    dfree(s->fout);
+    dfree(s->dump_count);
+    dfree(s->bond_idx);
+    dfree(s->bond_prm);
+    dfree(s->angle_idx);
+    dfree(s->angle_prm);
+    dfree(s->dih_idx);
+    dfree(s->dih_prm);
+    dfree(s->imp_idx);
+    dfree(s->imp_prm);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    delete s;
+    return MDG_OK;
+}
+
+MDG_API int mdg_system_set_stream(mdg_system *s, void *stream) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_system_set_box(mdg_system *s, const double *box) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!box) return fail(MDG_ERR_INVALID, "box is null");
+    rc = validate_box(box, s->nb_configured ? s->cutoff : 0.0);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    for (int d = 0; d < 3; ++d) s->box[d] = box[d];
+    rc = prepare_sort_grid(s);
+    if (rc) return fail(rc, "sort grid allocation failed");
+    if (s->pme.on) {
+        rc = pme_setup(s);
+        if (rc) return fail(rc, "PME set-up failed");
+    }
+    s->need_reorder = 1;
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_masses(mdg_system *s, const double *m) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    std::vector<double> mm(m, m + s->n), inv(s->n);
+    for (int i = 0; i < s->n; ++i) {
+        if (!(mm[i] > 0)) return fail(MDG_ERR_INVALID, "mass of atom %d is %g", i, mm[i]);
+        inv[i] = 1.0 / mm[i];
+    }
+    CK(cudaMemcpy(s->mass, mm.data(), sizeof(double) * s->n, cudaMemcpyHostToDevice), "copy");
+    CK(cudaMemcpy(s->inv_mass, inv.data(), sizeof(double) * s->n, cudaMemcpyHostToDevice), "copy");
+    s->have_masses = 1;
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_charges(mdg_system *s, const double *q) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    // q * sqrt(k_e): k_e = 1/(4 pi eps0) from mdpy's constants (mdpy/unit/__init__.py:56-58)
+    const double eps0 = 8.85418e-12 * 1.66053904e-27 / (1.602176634e-19 * 1.602176634e-19);
+    const double ke = 1.0 / (4.0 * 3.14159265358979323846 * eps0);
+    const double sk = std::sqrt(ke);
+    std::vector<float> qs(s->n);
+    double sum = 0.0, sum2 = 0.0;
+    for (int i = 0; i < s->n; ++i) {
+        qs[i] = (float)(q[i] * sk);
+        sum += q[i];
+        sum2 += q[i] * q[i];
+    }
+    CK(cudaMemcpy(s->charge, qs.data(), sizeof(float) * s->n, cudaMemcpyHostToDevice), "copy");
+    s->have_charges = 1;
+    s->need_reorder = 1;
+    s->forces_valid = 0;
+    drop_graph(s);
+    // FP64 Ewald constants depend on the charges
+    s->pme.e_self = 0.0;
+    s->pme.e_net = 0.0;
+    if (s->pme.beta > 0) {
+        const double V = s->box[0] * s->box[1] * s->box[2];
+        s->pme.e_self = -ke * s->pme.beta / std::sqrt(3.14159265358979323846) * sum2;
+        s->pme.e_net = -ke * 3.14159265358979323846 * sum * sum / (2.0 * s->pme.beta * s->pme.beta * V);
+    }
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_lj(mdg_system *s, const double *params) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    std::vector<float4> p(s->n);
+    for (int i = 0; i < s->n; ++i) {
+        const double *r = params + 4 * i;
+        if (r[0] < 0 || r[2] < 0) return fail(MDG_ERR_INVALID, "negative epsilon for atom %d", i);
+        p[i] = make_float4((float)(0.5 * r[1]), (float)std::sqrt(4.0 * r[0]), (float)(0.5 * r[3]),
+                           (float)std::sqrt(4.0 * r[2]));
+    }
+    CK(cudaMemcpy(s->lj, p.data(), sizeof(float4) * s->n, cudaMemcpyHostToDevice), "copy");
+    s->have_lj = 1;
+    s->need_reorder = 1;
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_exclusions(mdg_system *s, const int32_t *bonded, int bw,
+                               const int32_t *scaling, int sw) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    const int n = s->n;
+    if (bw < 0 || sw < 0) return fail(MDG_ERR_INVALID, "negative width");
+    // symmetric partner sets; a pair listed as both 1-2/1-3 and 1-4 stays excluded
+    std::vector<std::vector<int>> excl(n), p14(n);
+    auto add = [&](std::vector<std::vector<int>> &lst, int i, int j) {
+        if (j < 0) return 0;
+        if (j >= n || j == i) return 1;
+        if (std::find(lst[i].begin(), lst[i].end(), j) == lst[i].end()) lst[i].push_back(j);
+        if (std::find(lst[j].begin(), lst[j].end(), i) == lst[j].end()) lst[j].push_back(i);
+        return 0;
+    };
+    for (int i = 0; i < n; ++i) {
+        for (int w = 0; w < bw; ++w)
+            if (add(excl, i, bonded[(size_t)i * bw + w]))
+                return fail(MDG_ERR_INVALID, "bad bonded partner of atom %d", i);
+        for (int w = 0; w < sw; ++w)
+            if (add(p14, i, scaling[(size_t)i * sw + w]))
+                return fail(MDG_ERR_INVALID, "bad 1-4 partner of atom %d", i);
+    }
+    int pw = 0;
+    std::vector<int2> ex, s14;
+    for (int i = 0; i < n; ++i) {
+        auto &e = excl[i];
+        std::vector<int> p14only;
+        for (int j : p14[i])
+            if (std::find(e.begin(), e.end(), j) == e.end()) p14only.push_back(j);
+        p14[i] = p14only;
+        pw = std::max<int>(pw, (int)(e.size() + p14[i].size()));
+        for (int j : e)
+            if (j > i) ex.push_back(make_int2(i, j));
+        for (int j : p14[i])
+            if (j > i) s14.push_back(make_int2(i, j));
+    }
+    std::vector<int> flat((size_t)n * std::max(pw, 1), -1);
+    for (int i = 0; i < n; ++i) {
+        int w = 0;
+        for (int j : excl[i]) flat[(size_t)i * pw + w++] = j;
+        for (int j : p14[i]) flat[(size_t)i * pw + w++] = j | 0x40000000;
+    }
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    dfree(s->partners);
+    dfree(s->partners_sorted);
+    dfree(s->excl_pairs);
+    dfree(s->pairs14);
+    s->pw = pw;
+    if ((rc = dalloc(&s->partners, flat.size()))) return rc;
+    if ((rc = dalloc(&s->partners_sorted, (size_t)s->n_pad * std::max(pw, 1)))) return rc;
+    if ((rc = dalloc(&s->excl_pairs, ex.size()))) return rc;
+    if ((rc = dalloc(&s->pairs14, s14.size()))) return rc;
+    CK(cudaMemcpy(s->partners, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice), "copy");
+    if (!ex.empty())
+        CK(cudaMemcpy(s->excl_pairs, ex.data(), sizeof(int2) * ex.size(), cudaMemcpyHostToDevice), "copy");
+    if (!s14.empty())
+        CK(cudaMemcpy(s->pairs14, s14.data(), sizeof(int2) * s14.size(), cudaMemcpyHostToDevice), "copy");
+    s->n_excl = (int)ex.size();
+    s->n_14 = (int)s14.size();
+    s->need_reorder = 1;
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_nonbonded_config(mdg_system *s, double cutoff, double switch_radius, int lj_on,
+                                 int coulomb_mode, double beta) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (coulomb_mode < MDG_COUL_NONE || coulomb_mode > MDG_COUL_BARE)
+        return fail(MDG_ERR_INVALID, "unknown coulomb mode %d", coulomb_mode);
+    if (!(cutoff > 0)) return fail(MDG_ERR_CUTOFF, "cutoff must be positive");
+    rc = validate_box(s->box, cutoff);
+    if (rc) return rc;
+    if (coulomb_mode == MDG_COUL_EWALD && !(beta > 0))
+        return fail(MDG_ERR_INVALID, "Ewald mode needs beta > 0");
+    s->cutoff = (float)cutoff;
+    s->rswitch = (switch_radius > 0 && switch_radius < cutoff) ? (float)switch_radius : 0.0f;
+    s->lj_on = lj_on ? 1 : 0;
+    s->coul_mode = coulomb_mode;
+    s->beta = beta;
+    s->nb_configured = 1;
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_pme_config(mdg_system *s, const int *grid, int order, double beta) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!grid) return fail(MDG_ERR_INVALID, "grid is null");
+    if (order < 4 || order > 6) return fail(MDG_ERR_INVALID, "PME order %d not in 4..6", order);
+    for (int d = 0; d < 3; ++d)
+        if (grid[d] < 2 * order || grid[d] > 1024)
+            return fail(MDG_ERR_INVALID, "PME grid %d out of range", grid[d]);
+    if (!(beta > 0)) return fail(MDG_ERR_INVALID, "PME needs beta > 0");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    for (int d = 0; d < 3; ++d) s->pme.K[d] = grid[d];
+    s->pme.order = order;
+    s->pme.beta = beta;
+    rc = pme_setup(s);
+    if (rc) {
+        s->pme.on = 0;
+        return fail(rc, "PME set-up failed");
+    }
+    s->pme.on = 1;
+    // recompute the FP64 constants with this beta
+    std::vector<float> qs(s->n);
+    CK(cudaMemcpy(qs.data(), s->charge, sizeof(float) * s->n, cudaMemcpyDeviceToHost), "copy");
+    const double eps0 = 8.85418e-12 * 1.66053904e-27 / (1.602176634e-19 * 1.602176634e-19);
+    const double ke = 1.0 / (4.0 * 3.14159265358979323846 * eps0);
+    double sum = 0, sum2 = 0;
+    for (int i = 0; i < s->n; ++i) {
+        const double q = qs[i] / std::sqrt(ke);
+        sum += q;
+        sum2 += q * q;
+    }
+    const double V = s->box[0] * s->box[1] * s->box[2];
+    s->pme.e_self = -ke * beta / std::sqrt(3.14159265358979323846) * sum2;
+    s->pme.e_net = -ke * 3.14159265358979323846 * sum * sum / (2.0 * beta * beta * V);
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_reorder_interval(mdg_system *s, int steps) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (steps < 1 || steps > 100000) return fail(MDG_ERR_INVALID, "interval %d out of range", steps);
+    s->reorder_interval = steps;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+static int set_terms(mdg_system *s, int n, const int32_t *idx, const double *prm, int wi, int wp,
+                     int kind) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (n < 0) return fail(MDG_ERR_INVALID, "negative term count");
+    for (int t = 0; t < n * wi; ++t)
+        if (idx[t] < 0 || idx[t] >= s->n) return fail(MDG_ERR_INVALID, "term atom index out of range");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    if (kind == 0) {
+        std::vector<int2> I(n);
+        std::vector<float2> P(n);
+        for (int t = 0; t < n; ++t) {
+            I[t] = make_int2(idx[2 * t], idx[2 * t + 1]);
+            P[t] = make_float2((float)prm[2 * t], (float)prm[2 * t + 1]);
+        }
+        dfree(s->bond_idx);
+        dfree(s->bond_prm);
+        if ((rc = dalloc(&s->bond_idx, n)) || (rc = dalloc(&s->bond_prm, n))) return rc;
+        if (n) {
+            CK(cudaMemcpy(s->bond_idx, I.data(), sizeof(int2) * n, cudaMemcpyHostToDevice), "copy");
+            CK(cudaMemcpy(s->bond_prm, P.data(), sizeof(float2) * n, cudaMemcpyHostToDevice), "copy");
+        }
+        s->nb = n;
+    } else if (kind == 1) {
+        std::vector<int4> I(n);
+        std::vector<float4> P(n);
+        for (int t = 0; t < n; ++t) {
+            I[t] = make_int4(idx[3 * t], idx[3 * t + 1], idx[3 * t + 2], 0);
+            P[t] = make_float4((float)prm[4 * t], (float)prm[4 * t + 1], (float)prm[4 * t + 2],
+                               (float)prm[4 * t + 3]);
+        }
+        dfree(s->angle_idx);
+        dfree(s->angle_prm);
+        if ((rc = dalloc(&s->angle_idx, n)) || (rc = dalloc(&s->angle_prm, n))) return rc;
+        if (n) {
+            CK(cudaMemcpy(s->angle_idx, I.data(), sizeof(int4) * n, cudaMemcpyHostToDevice), "copy");
+            CK(cudaMemcpy(s->angle_prm, P.data(), sizeof(float4) * n, cudaMemcpyHostToDevice), "copy");
+        }
+        s->na = n;
+    } else if (kind == 2) {
+        std::vector<int4> I(n);
+        std::vector<float4> P(n);
+        for (int t = 0; t < n; ++t) {
+            I[t] = make_int4(idx[4 * t], idx[4 * t + 1], idx[4 * t + 2], idx[4 * t + 3]);
+            P[t] = make_float4((float)prm[3 * t], (float)prm[3 * t + 1], (float)prm[3 * t + 2], 0.f);
+        }
+        dfree(s->dih_idx);
+        dfree(s->dih_prm);
+        if ((rc = dalloc(&s->dih_idx, n)) || (rc = dalloc(&s->dih_prm, n))) return rc;
+        if (n) {
+            CK(cudaMemcpy(s->dih_idx, I.data(), sizeof(int4) * n, cudaMemcpyHostToDevice), "copy");
+            CK(cudaMemcpy(s->dih_prm, P.data(), sizeof(float4) * n, cudaMemcpyHostToDevice), "copy");
+        }
+        s->nd = n;
+    } else {
+        std::vector<int4> I(n);
+        std::vector<float2> P(n);
+        for (int t = 0; t < n; ++t) {
+            I[t] = make_int4(idx[4 * t], idx[4 * t + 1], idx[4 * t + 2], idx[4 * t + 3]);
+            P[t] = make_float2((float)prm[2 * t], (float)prm[2 * t + 1]);
+        }
+        dfree(s->imp_idx);
+        dfree(s->imp_prm);
+        if ((rc = dalloc(&s->imp_idx, n)) || (rc = dalloc(&s->imp_prm, n))) return rc;
+        if (n) {
+            CK(cudaMemcpy(s->imp_idx, I.data(), sizeof(int4) * n, cudaMemcpyHostToDevice), "copy");
+            CK(cudaMemcpy(s->imp_prm, P.data(), sizeof(float2) * n, cudaMemcpyHostToDevice), "copy");
+        }
+        s->ni = n;
+    }
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_bonds(mdg_system *s, int n, const int32_t *idx, const double *prm) {
+    return set_terms(s, n, idx, prm, 2, 2, 0);
+}
+MDG_API int mdg_set_angles(mdg_system *s, int n, const int32_t *idx, const double *prm) {
+    return set_terms(s, n, idx, prm, 3, 4, 1);
+}
+MDG_API int mdg_set_dihedrals(mdg_system *s, int n, const int32_t *idx, const double *prm) {
+    return set_terms(s, n, idx, prm, 4, 3, 2);
+}
+MDG_API int mdg_set_impropers(mdg_system *s, int n, const int32_t *idx, const double *prm) {
+    return set_terms(s, n, idx, prm, 4, 2, 3);
+}
+
+MDG_API int mdg_set_positions(mdg_system *s, const double *x, int where) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!x) return fail(MDG_ERR_INVALID, "positions pointer is null");
+    CK(cudaMemcpyAsync(s->x, x, sizeof(double) * 3 * s->n,
+                       where == MDG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       s->stream),
+       "copy positions");
+    if (where != MDG_DEVICE) CK(cudaStreamSynchronize(s->stream), "synchronize");
+    s->have_x = 1;
+    s->need_reorder = 1;
+    s->forces_valid = 0;
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_velocities(mdg_system *s, const double *v, int where) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!v) return fail(MDG_ERR_INVALID, "velocities pointer is null");
+    CK(cudaMemcpyAsync(s->v, v, sizeof(double) * 3 * s->n,
+                       where == MDG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       s->stream),
+       "copy velocities");
+    if (where != MDG_DEVICE) CK(cudaStreamSynchronize(s->stream), "synchronize");
+    s->have_v = 1;
+    return MDG_OK;
+}
+
+MDG_API int mdg_get_positions(mdg_system *s, double *x, int where) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!x) return fail(MDG_ERR_INVALID, "output pointer is null");
+    if (where == MDG_DEVICE) {
+        CK(launch_positions_out(s, x), "positions out");
+    } else {
+        CK(launch_positions_out(s, s->fout), "positions out");
+        CK(cudaMemcpyAsync(x, s->fout, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost,
+                           s->stream),
+           "copy");
+    }
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return read_status(s);
+}
+
+MDG_API int mdg_get_velocities(mdg_system *s, double *v, int where) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!v) return fail(MDG_ERR_INVALID, "output pointer is null");
+    CK(cudaMemcpyAsync(v, s->v, sizeof(double) * 3 * s->n,
+                       where == MDG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                       s->stream),
+       "copy velocities");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return MDG_OK;
+}
+
+MDG_API int mdg_compute_forces(mdg_system *s, unsigned mask) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    mask &= MDG_MASK_ALL;
+    rc = ready_for_forces(s, mask);
+    if (rc) return rc;
+    rc = evaluate(s, mask, 1);
+    if (rc) return rc;
+    s->forces_valid = 1;
+    s->forces_mask = mask;
+    CK(cudaGetLastError(), "compute forces");
+    return MDG_OK;
+}
+
+MDG_API int mdg_get_forces(mdg_system *s, double *f, int where) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!f) return fail(MDG_ERR_INVALID, "output pointer is null");
+    if (!s->forces_valid) return fail(MDG_ERR_STATE, "no force evaluation since the last change");
+    CK(launch_forces_out(s), "forces out");
+    CK(cudaMemcpyAsync(f, s->fout, sizeof(double) * 3 * s->n,
+                       where == MDG_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                       s->stream),
+       "copy forces");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return read_status(s);
+}
+
+MDG_API int mdg_get_energies(mdg_system *s, double *energies, double *kinetic) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    long long e[kEnergySlots];
+    CK(cudaMemcpyAsync(e, s->energy, sizeof(e), cudaMemcpyDeviceToHost, s->stream), "copy");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    rc = read_status(s);
+    if (rc) return rc;
+    if (energies) {
+        for (int t = 0; t < MDG_NUM_TERMS; ++t) energies[t] = (double)e[t] * kFixInv;
+        if ((s->forces_mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on)
+            energies[MDG_TERM_COUL_RECIP] += s->pme.e_self + s->pme.e_net;
+    }
+    if (kinetic) *kinetic = (double)e[kSlotKinetic] * kFixInv;
+    return MDG_OK;
+}
+
+MDG_API int mdg_kinetic_energy(mdg_system *s, double *kinetic) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(s->energy + kSlotKinetic, 0, sizeof(long long), s->stream), "memset");
+    CK(launch_kinetic(s), "kinetic");
+    long long e = 0;
+    CK(cudaMemcpyAsync(&e, s->energy + kSlotKinetic, sizeof(e), cudaMemcpyDeviceToHost, s->stream),
+       "copy");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    if (kinetic) *kinetic = (double)e * kFixInv;
+    return MDG_OK;
+}
+
+MDG_API int mdg_integrator_config(mdg_system *s, int kind, double dt, double temperature,
+                                  double friction, uint64_t seed) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (kind != MDG_INTEGRATOR_VERLET && kind != MDG_INTEGRATOR_LANGEVIN)
+        return fail(MDG_ERR_INVALID, "unknown integrator %d", kind);
+    if (!(dt > 0)) return fail(MDG_ERR_INVALID, "time step must be positive");
+    if (kind == MDG_INTEGRATOR_LANGEVIN && (!(temperature >= 0) || !(friction >= 0)))
+        return fail(MDG_ERR_INVALID, "temperature and friction must be >= 0");
+    s->integ_kind = kind;
+    s->dt = dt;
+    s->temperature = temperature;
+    s->friction = kind == MDG_INTEGRATOR_LANGEVIN ? friction : 0.0;
+    s->seed = seed;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_get_step(mdg_system *s, uint64_t *step) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (step) *step = s->step;
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_step(mdg_system *s, uint64_t step) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    unsigned long long v = step;
+    CK(cudaMemcpyAsync(s->step_dev, &v, sizeof(v), cudaMemcpyHostToDevice, s->stream), "copy");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    s->step = step;
+    return MDG_OK;
+}
+
+MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_energy) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (n_steps < 0) return fail(MDG_ERR_INVALID, "negative step count");
+    if (s->integ_kind < 0) return fail(MDG_ERR_STATE, "integrator has not been configured");
+    mask &= MDG_MASK_ALL;
+    rc = ready_for_forces(s, mask);
+    if (rc) return rc;
+    if (!s->have_masses) return fail(MDG_ERR_STATE, "masses have not been set");
+    if (!s->forces_valid || s->forces_mask != mask) {
+        rc = evaluate(s, mask, 1);
+        if (rc) return rc;
+        s->forces_valid = 1;
+        s->forces_mask = mask;
+    }
+    if (s->graph.exec && s->graph.mask != mask) drop_graph(s);
+    if (s->graph_step[0].exec && s->graph_step[0].mask != mask) drop_graph(s);
+    if (s->graph_step[1].exec && s->graph_step[1].mask != mask) drop_graph(s);
+    const int R = s->reorder_interval;
+    int remaining = n_steps;
+    while (remaining > 0) {
+        const bool chunk_start = s->need_reorder || s->steps_since_reorder >= R;
+        const int usable = remaining - (want_energy ? 1 : 0);
+        if (s->graph_mode == MDG_GRAPH_STEP && usable >= 1) {
+            Graph &g = s->graph_step[chunk_start ? 1 : 0];
+            if (!g.exec) {
+                rc = capture_steps(s, g, 1, chunk_start, mask);
+                if (rc) return rc;
+            }
+            CK(cudaGraphLaunch(g.exec, s->stream), "graph launch");
+            s->launches += g.steps;
+            s->need_reorder = 0;
+            s->steps_since_reorder = chunk_start ? 1 : s->steps_since_reorder + 1;
+            s->step += 1;
+            remaining -= 1;
+        } else if (chunk_start && usable >= R && R >= 2) {
+            if (!s->graph.exec) {
+                rc = capture_steps(s, s->graph, R, 1, mask);
+                if (rc) return rc;
+            }
+            CK(cudaGraphLaunch(s->graph.exec, s->stream), "graph launch");
+            s->launches += s->graph.steps;
+            s->need_reorder = 0;
+            s->steps_since_reorder = R;
+            s->step += R;
+            remaining -= R;
+        } else {
+            const int e = (want_energy && remaining == 1) ? 1 : 0;
+            rc = md_step(s, mask, e);
+            if (rc) return rc;
+            remaining -= 1;
+        }
+    }
+    if (want_energy && n_steps == 0) {
+        rc = evaluate(s, mask, 1);
+        if (rc) return rc;
+    }
+    s->forces_valid = 1;
+    s->forces_mask = mask;
+    CK(cudaGetLastError(), "integrate");
+    return MDG_OK;
+}
+
+MDG_API int mdg_pairset_dump(mdg_system *s, int32_t *pairs, int64_t capacity, int64_t *count) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    rc = ready_for_forces(s, MDG_MASK(MDG_TERM_LJ) | MDG_MASK(MDG_TERM_COUL_REAL));
+    if (rc) return rc;
+    if (capacity < 0) return fail(MDG_ERR_INVALID, "negative capacity");
+    if (s->need_reorder) {
+        CK(launch_reorder(s), "reorder");
+        s->need_reorder = 0;
+        s->steps_since_reorder = 0;
+    }
+    CK(launch_pack(s), "pack");
+    s->forces_valid = 0;  // pack zeroed the force slots
+    int *buf = nullptr;
+    if ((rc = dalloc(&buf, 2 * (size_t)std::max<int64_t>(capacity, 1)))) return rc;
+    s->dump_buf = buf;
+    s->dump_cap = capacity;
+    CK(cudaMemsetAsync(s->dump_count, 0, sizeof(unsigned long long), s->stream), "memset");
+    // the tile kernel covers LJ and Ewald real space; the pair set is the same
+    const int saved_mode = s->coul_mode, saved_lj = s->lj_on;
+    if (s->coul_mode == MDG_COUL_BARE) s->coul_mode = MDG_COUL_NONE;
+    s->lj_on = 1;
+    cudaError_t e = launch_nonbonded(s, MDG_MASK(MDG_TERM_LJ), 0, 1);
+    if (e == cudaSuccess) e = launch_special(s, MDG_MASK(MDG_TERM_LJ), 0, 1);
+    s->coul_mode = saved_mode;
+    s->lj_on = saved_lj;
+    unsigned long long got = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&got, s->dump_count, sizeof(got), cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess && pairs && capacity > 0)
+        e = cudaMemcpy(pairs, buf, sizeof(int) * 2 * std::min<int64_t>(capacity, (int64_t)got),
+                       cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    s->dump_buf = nullptr;
+    s->dump_cap = 0;
+    if (e != cudaSuccess) return cuda_fail(e, "pair dump");
+    if (count) *count = (int64_t)got;
+    if ((int64_t)got > capacity) return fail(MDG_ERR_CAPACITY, "%lld pairs exceed capacity %lld",
+                                             (long long)got, (long long)capacity);
+    return MDG_OK;
+}
+
+MDG_API int mdg_langevin_noise(mdg_system *s, uint64_t step, float *out) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!out) return fail(MDG_ERR_INVALID, "output pointer is null");
+    float *d = nullptr;
+    if ((rc = dalloc(&d, 3 * (size_t)s->n))) return rc;
+    cudaError_t e = launch_noise(s, step, d);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, d, sizeof(float) * 3 * s->n, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "noise");
+    return MDG_OK;
+}
+
+MDG_API int mdg_check_status(mdg_system *s) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return read_status(s);
+}
+
+MDG_API int mdg_nonbonded_stats(mdg_system *s, int64_t *stats) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    unsigned long long v[4];
+    CK(cudaMemcpyAsync(v, s->stats, sizeof(v), cudaMemcpyDeviceToHost, s->stream), "copy");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    for (int k = 0; k < 4; ++k) stats[k] = (int64_t)v[k];
+    return MDG_OK;
+}
+
+MDG_API int mdg_set_graph_mode(mdg_system *s, int mode) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (mode != MDG_GRAPH_CHUNK && mode != MDG_GRAPH_STEP)
+        return fail(MDG_ERR_INVALID, "unknown graph mode %d", mode);
+    s->graph_mode = mode;
+    return MDG_OK;
+}
+
+MDG_API int mdg_launch_stage(mdg_system *s, int stage, unsigned mask) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!s->forces_valid && stage != MDG_STAGE_REORDER && stage != MDG_STAGE_PACK)
+        return fail(MDG_ERR_STATE, "evaluate the system once before launching single stages");
+    mask &= MDG_MASK_ALL;
+    switch (stage) {
+        case MDG_STAGE_PACK: CK(launch_pack(s), "pack"); break;
+        case MDG_STAGE_NONBONDED: CK(launch_nonbonded(s, mask, 0, 0), "nonbonded"); break;
+        case MDG_STAGE_SPECIAL: CK(launch_special(s, mask, 0, 0), "special"); break;
+        case MDG_STAGE_PME: {
+            if (!s->pme.on) return fail(MDG_ERR_STATE, "PME is not configured");
+            int cr = 0;
+            cudaError_t e = launch_pme(s, 0, &cr);
+            if (cr != CUFFT_SUCCESS) return fail(MDG_ERR_CUFFT, "cuFFT execution failed (%d)", cr);
+            CK(e, "pme");
+            break;
+        }
+        case MDG_STAGE_BONDED: CK(launch_bonded(s, mask, 0), "bonded"); break;
+        case MDG_STAGE_REORDER: CK(launch_reorder(s), "reorder"); break;
+        case MDG_STAGE_INTEGRATE:
+            if (s->integ_kind < 0) return fail(MDG_ERR_STATE, "integrator not configured");
+            CK(launch_integrate_pre(s), "pre");
+            CK(launch_integrate_post(s, 0), "post");
+            break;
+        default: return fail(MDG_ERR_INVALID, "unknown stage %d", stage);
+    }
+    if (stage != MDG_STAGE_REORDER && stage != MDG_STAGE_INTEGRATE) s->forces_valid = 0;
+    return MDG_OK;
+}
+
+MDG_API int mdg_launch_count(mdg_system *s, int64_t *count) {
+    if (!s) return fail(MDG_ERR_INVALID, "null system");
+    if (count) *count = s->launches;
+    return MDG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,658 @@
+// mdg_nonbonded.cu -- short-range nonbonded forces.
+//
+// Replaces, for the pair work:
+//   CharmmNonbondedConstraint.cpu_kernel / cuda_kernel
+//     (mdpy/constraint/charmm_nonbonded_constraint.py:64-181): LJ 12-6 with
+//     Lorentz-Berthelot combination, 1-4 parameters for scaling_particles,
+//     bonded_particles excluded, hard cutoff r <= rc;
+//   ElectrostaticConstraint (mdpy/constraint/electrostatic_constraint.py:52-135):
+//     bare Coulomb, all pairs, minimum image (kept as MDG_COUL_BARE for parity);
+// and adds the Ewald real-space term k q_i q_j erfc(beta r)/r (MDG_COUL_EWALD),
+// which mdpy v0.2.1 does not have, plus an optional CHARMM switch for LJ.
+//
+// Design (GB300): one CTA of 4 warps per 32-atom i-cluster I.
+//   1. warp 0 walks the cluster bounding boxes J >= I (half shell) and keeps,
+//      in shared memory, every (J, periodic image) whose box lies within rc
+//      of I's box -- candidate compaction with __ballot_sync;
+//   2. the 4 warps take candidates round-robin; for each, every lane tests one
+//      j atom against I's bounding box, and the survivors are appended (warp
+//      ballot + popc, no atomics) to a 64-entry per-warp ring buffer in
+//      shared memory, already shifted to the right periodic image and with a
+//      32-bit exclusion mask (which i lanes must skip this j);
+//   3. each full chunk of 32 j entries is swept against the warp's 32 i atoms
+//      in 32 rotation steps: at step t lane l pairs its i atom with entry
+//      (l+t) mod 32, keeps the i force in registers and passes the j force
+//      accumulator to lane l-1 with one shuffle per component, so after the
+//      sweep every lane owns one entry's complete j force.  No shared-memory
+//      atomics, no per-pair reduction trees.
+// Forces leave as int64 fixed point (scale 2^32) through 64-bit global
+// atomics: the sum is independent of the order of arrival, so results are
+// bit-reproducible run to run.  Pairs are never stored: the pair set is
+// found afresh from the current coordinates on every evaluation, so no
+// Verlet skin or rebuild criterion exists that could miss a pair.
+#include "mdg_internal.cuh"
+
+namespace mdg {
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kCandCap = 2048;
+constexpr int kRing = 64;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Abramowitz & Stegun 7.1.26: erfc(x) ~ t(a1 + t(a2 + t(a3 + t(a4 + t a5)))) e^{-x^2},
+// t = 1/(1 + p x), |error| <= 1.5e-7
+constexpr float kAsP = 0.3275911f;
+constexpr float kAsA1 = 0.254829592f, kAsA2 = -0.284496736f, kAsA3 = 1.421413741f,
+                kAsA4 = -1.453152027f, kAsA5 = 1.061405429f;
+
+struct NbArgs {
+    const float4 *__restrict__ xq;
+    const float2 *__restrict__ prm;
+    const int *__restrict__ partners;
+    int pw;
+    const int2 *__restrict__ prange;
+    const float4 *__restrict__ bbox;
+    int n, n_pad, n_clusters;
+    float L[3], invL[3];
+    float rc, rc2, rs2, sw_inv_den;
+    float beta_p;        // A&S p * beta
+    float ewald_exp_c;   // beta^2 log2(e)
+    float ewald_fc;      // 2 beta / sqrt(pi)
+    int lj_on;
+    unsigned long long *f;
+    long long *energy;
+    int *status;
+    unsigned long long *stats;
+    int *dump;
+    long long dump_cap;
+    unsigned long long *dump_count;
+    const int *perm;
+};
+
+__device__ __forceinline__ void decode_shift(int code, const NbArgs &a, float &sx, float &sy,
+                                             float &sz) {
+    sx = (float)(code / 9 - 1) * a.L[0];
+    sy = (float)((code / 3) % 3 - 1) * a.L[1];
+    sz = (float)(code % 3 - 1) * a.L[2];
+}
+
+template <int COUL, bool SWITCH, bool ENERGY, bool DUMP>
+__global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
+    __shared__ int s_cand[kCandCap];
+    __shared__ int s_ncand, s_next;
+    __shared__ float4 s_jx[kWarps][kRing];
+    __shared__ float2 s_jp[kWarps][kRing];
+    __shared__ int2 s_jm[kWarps][kRing];
+    __shared__ float s_fi[3][kWarps][32];
+    __shared__ float s_e[2][kWarps];
+
+    const int I = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int ik = I * kCluster + lane;
+    const float4 xi = a.xq[ik];
+    const float2 pi = a.prm[ik];
+    const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
+    const int2 rI = a.prange[I];
+    const int ilo = I * kCluster;
+
+    float fix = 0.f, fiy = 0.f, fiz = 0.f;
+    float acc_lj = 0.f, acc_c = 0.f;
+    unsigned long long n_eval = 0, n_in = 0;
+    int jbase = 0, jcount = 0;
+
+    // sweep of one 32-entry chunk starting at ring slot `base`
+    auto chunk = [&](int base) {
+        float fjx = 0.f, fjy = 0.f, fjz = 0.f;
+#pragma unroll 4
+        for (int t = 0; t < 32; ++t) {
+            const int e = (base + ((lane + t) & 31)) & (kRing - 1);
+            const float4 xj = s_jx[warp][e];
+            const float2 pj = s_jp[warp][e];
+            const unsigned mk = (unsigned)s_jm[warp][e].y;
+            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const bool inc = (r2 <= a.rc2) && !((mk >> lane) & 1u);
+            if (DUMP && inc) {
+                unsigned long long slot = atomicAdd(a.dump_count, 1ull);
+                if ((long long)slot < a.dump_cap) {
+                    int pj_atom = a.perm[s_jm[warp][e].x], pi_atom = a.perm[ik];
+                    a.dump[2 * slot] = min(pi_atom, pj_atom);
+                    a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
+                }
+            }
+            const float r2s = inc ? r2 : 1.0f;
+            const float rinv = rsqrtf(r2s);
+            const float rinv2 = rinv * rinv;
+            float fr = 0.f, elj = 0.f, ecl = 0.f;
+            if (a.lj_on) {
+                const float sig = pi.x + pj.x;
+                const float s2 = sig * sig * rinv2;
+                const float s6 = s2 * s2 * s2;
+                const float c6 = pi.y * pj.y * s6;
+                elj = c6 * (s6 - 1.0f);
+                float flj = c6 * fmaf(12.0f, s6, -6.0f) * rinv2;
+                if (SWITCH) {
+                    if (r2s > a.rs2) {
+                        const float u = a.rc2 - r2s;
+                        const float sw = u * u * fmaf(2.0f, r2s, a.rc2 - 3.0f * a.rs2) * a.sw_inv_den;
+                        const float dsw = 12.0f * u * (a.rs2 - r2s) * a.sw_inv_den;
+                        flj = flj * sw - elj * dsw;
+                        elj *= sw;
+                    }
+                }
+                fr = flj;
+            }
+            if (COUL == MDG_COUL_EWALD) {
+                const float qq = xi.w * xj.w;
+                const float r = r2s * rinv;
+                const float tt = __fdividef(1.0f, fmaf(a.beta_p, r, 1.0f));
+                const float poly =
+                    tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, kAsA5, kAsA4), kAsA3), kAsA2), kAsA1);
+                const float ex = exp2f(-a.ewald_exp_c * r2s);
+                ecl = qq * poly * ex * rinv;
+                fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecl), rinv2, fr);
+            }
+            fr = inc ? fr : 0.f;
+            fix = fmaf(-fr, dx, fix);
+            fiy = fmaf(-fr, dy, fiy);
+            fiz = fmaf(-fr, dz, fiz);
+            fjx = fmaf(fr, dx, fjx);
+            fjy = fmaf(fr, dy, fjy);
+            fjz = fmaf(fr, dz, fjz);
+            if (ENERGY) {
+                acc_lj += inc ? elj : 0.f;
+                acc_c += inc ? ecl : 0.f;
+                n_in += __popc(__ballot_sync(kFull, inc));
+            }
+            const int src = (lane + 1) & 31;
+            fjx = __shfl_sync(kFull, fjx, src);
+            fjy = __shfl_sync(kFull, fjy, src);
+            fjz = __shfl_sync(kFull, fjz, src);
+        }
+        const int e = (base + lane) & (kRing - 1);
+        const int jk = s_jm[warp][e].x;
+        if (jk >= 0 && !DUMP) {
+            if (!(fabsf(fjx) < kFixLimit && fabsf(fjy) < kFixLimit && fabsf(fjz) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            fix_red(&a.f[jk], to_fix(fjx));
+            fix_red(&a.f[a.n_pad + jk], to_fix(fjy));
+            fix_red(&a.f[2 * a.n_pad + jk], to_fix(fjz));
+        }
+        n_eval += 32;
+        __syncwarp();
+    };
+
+    int Jstart = I;
+    for (;;) {
+        // ---- 1. cluster candidates (warp 0) -----------------------------
+        if (warp == 0) {
+            int nc = 0;
+            int J0 = Jstart;
+            for (; J0 < a.n_clusters; J0 += 32) {
+                const int J = J0 + lane;
+                const bool valid = J < a.n_clusters;
+                float4 cJ = make_float4(0.f, 0.f, 0.f, 0.f), hJ = cJ;
+                if (valid) {
+                    cJ = a.bbox[2 * J];
+                    hJ = a.bbox[2 * J + 1];
+                }
+                const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+                const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+                int ncode = 0;
+                float g2 = 0.f;
+                bool multi = false;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float nk = -rintf(d[k] * a.invL[k]);
+                    nk = fminf(fmaxf(nk, -1.f), 1.f);
+                    const float dd = fmaf(nk, a.L[k], d[k]);
+                    const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                    g2 = fmaf(gap, gap, g2);
+                    ncode = ncode * 3 + (int)nk + 1;
+                    multi = multi || (h[k] + a.rc >= 0.5f * a.L[k]);
+                }
+                multi = multi && valid;
+                const bool near_hit = valid && g2 <= a.rc2;
+                const bool any_multi = __any_sync(kFull, multi);
+                if (nc + (any_multi ? 32 * 27 : 32) > kCandCap) break;  // next round
+                if (any_multi) {
+                    for (int code = 0; code < 27; ++code) {
+                        bool hit;
+                        if (multi) {
+                            const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
+                            float gg = 0.f;
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) {
+                                const float dd = fmaf((float)s3[k], a.L[k], d[k]);
+                                const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                                gg = fmaf(gap, gap, gg);
+                            }
+                            hit = gg <= a.rc2;
+                        } else {
+                            hit = near_hit && code == ncode;
+                        }
+                        const unsigned b = __ballot_sync(kFull, hit);
+                        if (hit) s_cand[nc + __popc(b & lt)] = (J << 5) | code;
+                        nc += __popc(b);
+                    }
+                } else {
+                    const unsigned b = __ballot_sync(kFull, near_hit);
+                    if (near_hit) s_cand[nc + __popc(b & lt)] = (J << 5) | ncode;
+                    nc += __popc(b);
+                }
+            }
+            if (lane == 0) {
+                s_ncand = nc;
+                s_next = J0;
+            }
+        }
+        __syncthreads();
+        const int ncand = s_ncand, next = s_next;
+
+        // ---- 2./3. atom compaction and chunk sweeps ---------------------
+        for (int c = warp; c < ncand; c += kWarps) {
+            const int cc = s_cand[c];
+            const int J = cc >> 5;
+            float sx, sy, sz;
+            decode_shift(cc & 31, a, sx, sy, sz);
+            const int jk = J * kCluster + lane;
+            float4 xj = a.xq[jk];
+            xj.x += sx;
+            xj.y += sy;
+            xj.z += sz;
+            const float gx = fmaxf(fabsf(xj.x - cI.x) - hI.x, 0.f);
+            const float gy = fmaxf(fabsf(xj.y - cI.y) - hI.y, 0.f);
+            const float gz = fmaxf(fabsf(xj.z - cI.z) - hI.z, 0.f);
+            const bool hit = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) <= a.rc2;
+            const unsigned b = __ballot_sync(kFull, hit);
+            if (b == 0u) continue;
+            unsigned m = 0u;
+            if (hit) {
+                if (J == I) m = kFull << lane;  // half shell inside the cluster
+                if (rI.y >= J * kCluster && rI.x < (J + 1) * kCluster) {
+                    for (int w = 0; w < a.pw; ++w) {
+                        const int p = a.partners[(size_t)jk * a.pw + w];
+                        if (p >= 0) {
+                            const int pk = (p & 0x3fffffff) - ilo;
+                            if (pk >= 0 && pk < kCluster) m |= 1u << pk;
+                        }
+                    }
+                }
+                const int pos = (jbase + jcount + __popc(b & lt)) & (kRing - 1);
+                s_jx[warp][pos] = xj;
+                s_jp[warp][pos] = a.prm[jk];
+                s_jm[warp][pos] = make_int2(jk, (int)m);
+            }
+            jcount += __popc(b);
+            __syncwarp();
+            if (jcount >= 32) {
+                chunk(jbase);
+                jbase = (jbase + 32) & (kRing - 1);
+                jcount -= 32;
+            }
+        }
+        __syncthreads();
+        if (next >= a.n_clusters) break;
+        Jstart = next;
+    }
+    if (jcount > 0) {
+        const int pos = (jbase + lane) & (kRing - 1);
+        if (lane >= jcount) {
+            s_jx[warp][pos] = make_float4(kFarAway, kFarAway, kFarAway, 0.f);
+            s_jp[warp][pos] = make_float2(0.f, 0.f);
+            s_jm[warp][pos] = make_int2(-1, (int)kFull);
+        }
+        __syncwarp();
+        chunk(jbase);
+    }
+
+    // ---- i forces and energies ------------------------------------------
+    s_fi[0][warp][lane] = fix;
+    s_fi[1][warp][lane] = fiy;
+    s_fi[2][warp][lane] = fiz;
+    if (ENERGY) {
+        const float el = warp_sum(acc_lj), ee = warp_sum(acc_c);
+        if (lane == 0) {
+            s_e[0][warp] = el;
+            s_e[1][warp] = ee;
+        }
+    }
+    __syncthreads();
+    if (warp == 0 && !DUMP) {
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            sx += s_fi[0][w][lane];
+            sy += s_fi[1][w][lane];
+            sz += s_fi[2][w][lane];
+        }
+        if (ik < a.n) {
+            if (!(fabsf(sx) < kFixLimit && fabsf(sy) < kFixLimit && fabsf(sz) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            fix_red(&a.f[ik], to_fix(sx));
+            fix_red(&a.f[a.n_pad + ik], to_fix(sy));
+            fix_red(&a.f[2 * a.n_pad + ik], to_fix(sz));
+        }
+        if (ENERGY && lane == 0) {
+            float el = 0.f, ee = 0.f;
+            for (int w = 0; w < kWarps; ++w) {
+                el += s_e[0][w];
+                ee += s_e[1][w];
+            }
+            if (!(fabsf(el) < kFixLimit && fabsf(ee) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix(el));
+            fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix(ee));
+        }
+    }
+    if (ENERGY && lane == 0) {
+        atomicAdd(&a.stats[0], n_eval);
+        atomicAdd(&a.stats[1], n_in);
+        if (warp == 0) {
+            atomicAdd(&a.stats[2], (unsigned long long)s_ncand);
+            atomicAdd(&a.stats[3], 1ull);
+        }
+    }
+}
+
+// Bare Coulomb over all pairs with the minimum image (parity path for
+// ElectrostaticConstraint, electrostatic_constraint.py:52-79): one thread per
+// i atom, j atoms staged through shared memory in tiles, forces on i only.
+__global__ void __launch_bounds__(256) k_coulomb_bare(NbArgs a) {
+    __shared__ float4 s_x[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool iv = i < a.n;
+    const float4 xi = iv ? a.xq[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+    for (int base = 0; base < a.n; base += 256) {
+        const int jl = base + threadIdx.x;
+        s_x[threadIdx.x] = jl < a.n ? a.xq[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        const int lim = min(256, a.n - base);
+        if (iv) {
+            for (int t = 0; t < lim; ++t) {
+                const int j = base + t;
+                if (j == i) continue;
+                bool excl = false;
+                for (int w = 0; w < a.pw; ++w) {
+                    const int p = a.partners[(size_t)i * a.pw + w];
+                    if (p >= 0 && !(p & 0x40000000) && p == j) excl = true;
+                }
+                if (excl) continue;
+                const float4 xj = s_x[t];
+                float d[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float sc = d[k] * a.invL[k];
+                    d[k] = (sc - rintf(sc)) * a.L[k];
+                }
+                const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                const float rinv = rsqrtf(r2);
+                const float qq = xi.w * xj.w;
+                const float ev = qq * rinv;
+                const float fr = ev * rinv * rinv;
+                e += 0.5f * ev;
+                fx -= fr * d[0];
+                fy -= fr * d[1];
+                fz -= fr * d[2];
+            }
+        }
+        __syncthreads();
+    }
+    if (iv) {
+        fix_red(&a.f[i], to_fix(fx));
+        fix_red(&a.f[a.n_pad + i], to_fix(fy));
+        fix_red(&a.f[2 * a.n_pad + i], to_fix(fz));
+    }
+    __shared__ float s_e[8];
+    e = warp_sum(e);
+    if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_e[w];
+        fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix(t));
+    }
+}
+
+// ---- special pairs ---------------------------------------------------------
+struct SpArgs {
+    const double *__restrict__ x;
+    const int *__restrict__ inv_perm;
+    const float *__restrict__ charge;  // q * sqrt(k_e), atom order
+    const float4 *__restrict__ lj;     // atom order
+    const int2 *__restrict__ excl;
+    const int2 *__restrict__ p14;
+    int n_excl, n_14, n_pad;
+    double L[3];
+    float rc2, rs2, sw_inv_den, beta, ewald_fc;
+    int do_excl, do_lj14, do_coul14;
+    unsigned long long *f;
+    long long *energy;
+    int *dump;
+    long long dump_cap;
+    unsigned long long *dump_count;
+};
+
+// Excluded 1-2/1-3 pairs: -k q q erf(beta r)/r removes their share of the
+// reciprocal sum (term COUL_RECIP).  1-4 pairs: LJ with the 1-4 parameters
+// (charmm_nonbonded_constraint.py:92-97) and the real-space Coulomb term.
+template <bool SWITCH, bool DUMP>
+__global__ void k_special(SpArgs a) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    float e_lj = 0.f, e_cr = 0.f, e_rec = 0.f;
+    if (t < a.n_excl + a.n_14) {
+        const bool is14 = t >= a.n_excl;
+        const int2 pr = is14 ? a.p14[t - a.n_excl] : a.excl[t];
+        const int i = pr.x, j = pr.y;
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double dd = a.x[3 * j + k] - a.x[3 * i + k];
+            dd -= a.L[k] * rint(dd / a.L[k]);
+            d[k] = (float)dd;
+        }
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const float r = sqrtf(r2);
+        const float qq = a.charge[i] * a.charge[j];
+        float fr = 0.f;
+        if (!is14) {
+            if (a.do_excl) {
+                const float br = a.beta * r;
+                const float ef = erff(br);
+                e_rec = -qq * ef / r;
+                fr = qq * (a.ewald_fc * expf(-br * br) * r - ef) / (r2 * r);
+            }
+        } else if (r2 <= a.rc2) {
+            if (DUMP) {
+                unsigned long long slot = atomicAdd(a.dump_count, 1ull);
+                if ((long long)slot < a.dump_cap) {
+                    a.dump[2 * slot] = min(i, j);
+                    a.dump[2 * slot + 1] = max(i, j);
+                }
+            }
+            if (a.do_lj14) {
+                const float4 pi = a.lj[i], pj = a.lj[j];
+                const float sig = pi.z + pj.z;
+                const float s2 = sig * sig / r2;
+                const float s6 = s2 * s2 * s2;
+                const float c6 = pi.w * pj.w * s6;
+                float elj = c6 * (s6 - 1.0f);
+                float flj = c6 * (12.0f * s6 - 6.0f) / r2;
+                if (SWITCH && r2 > a.rs2) {
+                    const float u = a.rc2 - r2;
+                    const float sw = u * u * (a.rc2 + 2.0f * r2 - 3.0f * a.rs2) * a.sw_inv_den;
+                    const float dsw = 12.0f * u * (a.rs2 - r2) * a.sw_inv_den;
+                    flj = flj * sw - elj * dsw;
+                    elj *= sw;
+                }
+                e_lj = elj;
+                fr += flj;
+            }
+            if (a.do_coul14) {
+                const float br = a.beta * r;
+                const float ec = erfcf(br);
+                e_cr = qq * ec / r;
+                fr += qq * (ec / r + a.ewald_fc * expf(-br * br)) / r2;
+            }
+        }
+        if (!DUMP && fr != 0.f) {
+            const int ki = a.inv_perm[i], kj = a.inv_perm[j];
+            fix_red(&a.f[kj], to_fix(fr * d[0]));
+            fix_red(&a.f[a.n_pad + kj], to_fix(fr * d[1]));
+            fix_red(&a.f[2 * a.n_pad + kj], to_fix(fr * d[2]));
+            fix_red(&a.f[ki], to_fix(-fr * d[0]));
+            fix_red(&a.f[a.n_pad + ki], to_fix(-fr * d[1]));
+            fix_red(&a.f[2 * a.n_pad + ki], to_fix(-fr * d[2]));
+        }
+    }
+    if (DUMP) return;
+    __shared__ float s_e[3][8];
+    e_lj = warp_sum(e_lj);
+    e_cr = warp_sum(e_cr);
+    e_rec = warp_sum(e_rec);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_e[0][w] = e_lj;
+        s_e[1][w] = e_cr;
+        s_e[2][w] = e_rec;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            a0 += s_e[0][k];
+            a1 += s_e[1][k];
+            a2 += s_e[2][k];
+        }
+        if (a0 != 0.f) fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix(a0));
+        if (a1 != 0.f) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix(a1));
+        if (a2 != 0.f) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_RECIP], to_fix(a2));
+    }
+}
+
+NbArgs make_args(mdg_system *s) {
+    NbArgs a;
+    a.xq = s->xq;
+    a.prm = s->prm_sorted;
+    a.partners = s->partners_sorted;
+    a.pw = s->pw;
+    a.prange = s->cluster_partner_range;
+    a.bbox = s->bbox;
+    a.n = s->n;
+    a.n_pad = s->n_pad;
+    a.n_clusters = s->n_clusters;
+    for (int k = 0; k < 3; ++k) {
+        a.L[k] = (float)s->box[k];
+        a.invL[k] = (float)(1.0 / s->box[k]);
+    }
+    a.rc = s->cutoff;
+    a.rc2 = s->cutoff * s->cutoff;
+    const double rs = s->rswitch > 0 ? s->rswitch : s->cutoff;
+    a.rs2 = (float)(rs * rs);
+    const double den = (double)a.rc2 - rs * rs;
+    a.sw_inv_den = den > 0 ? (float)(1.0 / (den * den * den)) : 0.f;
+    a.beta_p = kAsP * (float)s->beta;
+    a.ewald_exp_c = (float)(s->beta * s->beta * 1.4426950408889634);
+    a.ewald_fc = (float)(2.0 * s->beta / 1.7724538509055159);
+    a.lj_on = s->lj_on;
+    a.f = s->f;
+    a.energy = s->energy;
+    a.status = s->status;
+    a.stats = s->stats;
+    a.dump = s->dump_buf;
+    a.dump_cap = s->dump_cap;
+    a.dump_count = s->dump_count;
+    a.perm = s->perm;
+    return a;
+}
+
+template <int COUL, bool SW>
+cudaError_t dispatch_nb(mdg_system *s, const NbArgs &a, int energy, int dump) {
+    dim3 grid(s->n_clusters), block(kWarps * 32);
+    if (dump)
+        k_nonbonded<COUL, SW, false, true><<<grid, block, 0, s->stream>>>(a);
+    else if (energy)
+        k_nonbonded<COUL, SW, true, false><<<grid, block, 0, s->stream>>>(a);
+    else
+        k_nonbonded<COUL, SW, false, false><<<grid, block, 0, s->stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_nonbonded(mdg_system *s, unsigned mask, int energy, int dump) {
+    const bool want_lj = (mask & MDG_MASK(MDG_TERM_LJ)) && s->lj_on;
+    const bool want_c = (mask & MDG_MASK(MDG_TERM_COUL_REAL)) && s->coul_mode != MDG_COUL_NONE;
+    if (!want_lj && !want_c) return cudaSuccess;
+    NbArgs a = make_args(s);
+    a.lj_on = want_lj ? 1 : 0;
+    const bool sw = s->rswitch > 0 && s->rswitch < s->cutoff;
+    cudaError_t err = cudaSuccess;
+    const int coul_tile = (want_c && s->coul_mode == MDG_COUL_EWALD) ? MDG_COUL_EWALD : MDG_COUL_NONE;
+    if (want_lj || coul_tile == MDG_COUL_EWALD) {
+        if (coul_tile == MDG_COUL_EWALD)
+            err = sw ? dispatch_nb<MDG_COUL_EWALD, true>(s, a, energy, dump)
+                     : dispatch_nb<MDG_COUL_EWALD, false>(s, a, energy, dump);
+        else
+            err = sw ? dispatch_nb<MDG_COUL_NONE, true>(s, a, energy, dump)
+                     : dispatch_nb<MDG_COUL_NONE, false>(s, a, energy, dump);
+        s->launches += 1;
+        if (err != cudaSuccess) return err;
+    }
+    if (want_c && s->coul_mode == MDG_COUL_BARE && !dump) {
+        k_coulomb_bare<<<(s->n + 255) / 256, 256, 0, s->stream>>>(a);
+        s->launches += 1;
+        err = cudaGetLastError();
+    }
+    return err;
+}
+
+cudaError_t launch_special(mdg_system *s, unsigned mask, int energy, int dump) {
+    (void)energy;
+    SpArgs a;
+    a.x = s->x;
+    a.inv_perm = s->inv_perm;
+    a.charge = s->charge;
+    a.lj = s->lj;
+    a.excl = s->excl_pairs;
+    a.p14 = s->pairs14;
+    a.n_excl = s->n_excl;
+    a.n_14 = s->n_14;
+    a.n_pad = s->n_pad;
+    for (int k = 0; k < 3; ++k) a.L[k] = s->box[k];
+    a.rc2 = s->cutoff * s->cutoff;
+    const double rs = s->rswitch > 0 ? s->rswitch : s->cutoff;
+    a.rs2 = (float)(rs * rs);
+    const double den = (double)a.rc2 - rs * rs;
+    a.sw_inv_den = den > 0 ? (float)(1.0 / (den * den * den)) : 0.f;
+    a.beta = (float)s->beta;
+    a.ewald_fc = (float)(2.0 * s->beta / 1.7724538509055159);
+    a.do_excl = (mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on && !dump;
+    a.do_lj14 = (mask & MDG_MASK(MDG_TERM_LJ)) && s->lj_on;
+    a.do_coul14 = (mask & MDG_MASK(MDG_TERM_COUL_REAL)) && s->coul_mode == MDG_COUL_EWALD;
+    a.f = s->f;
+    a.energy = s->energy;
+    a.dump = s->dump_buf;
+    a.dump_cap = s->dump_cap;
+    a.dump_count = s->dump_count;
+    if (!dump && !a.do_lj14 && !a.do_coul14) a.n_14 = 0;
+    if (!a.do_excl) a.n_excl = 0;
+    if (dump && !(a.do_lj14 || a.do_coul14)) a.n_14 = 0;
+    const int total = a.n_excl + a.n_14;
+    if (total == 0) return cudaSuccess;
+    const bool sw = s->rswitch > 0 && s->rswitch < s->cutoff;
+    const int tb = 256, nb = (total + tb - 1) / tb;
+    if (dump)
+        sw ? k_special<true, true><<<nb, tb, 0, s->stream>>>(a)
+           : k_special<false, true><<<nb, tb, 0, s->stream>>>(a);
+    else
+        sw ? k_special<true, false><<<nb, tb, 0, s->stream>>>(a)
+           : k_special<false, false><<<nb, tb, 0, s->stream>>>(a);
+    s->launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace mdg

@@ -1,0 +1,336 @@
+// mdg_sort.cu -- spatial sort of atoms into 32-atom clusters, and the per-step
+// pack of cluster coordinates and bounding boxes.
+//
+// Replaces mdpy's CellList (mdpy/core/cell_list.py:83-116), which rebuilds a
+// dense padded (nx, ny, nz, max_per_cell) cell list from scratch on every
+// State.set_positions.  Here the atoms are re-sorted every `reorder_interval`
+// steps into Z-order (Morton) of fine cells so that each run of 32 sorted
+// atoms is a spatially compact cluster; between sorts only the cluster
+// bounding boxes are refreshed (k_pack).  Neighbour candidates are found on
+// the fly from those boxes in the pair kernel, so the sort interval affects
+// only efficiency, never which pairs are found.
+//
+// The sort is a deterministic counting sort: histogram of cell keys,
+// exclusive scan, scatter, then an insertion sort by atom index inside each
+// (small) cell, so a given configuration always yields the same order.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mdg_internal.cuh"
+
+namespace mdg {
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanPerBlock = 2 * kScanThreads;
+
+__global__ void k_bin(double *__restrict__ x, int n, double bx, double by, double bz, int ncx,
+                      int ncy, int ncz, const int *__restrict__ cell_rank, int *__restrict__ key,
+                      int *__restrict__ count, int *__restrict__ status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double L[3] = {bx, by, bz};
+    const int nc[3] = {ncx, ncy, ncz};
+    int c[3];
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double p = x[3 * i + d];
+        ok = ok && isfinite(p);
+        p -= L[d] * floor(p / L[d]);
+        if (p >= L[d]) p -= L[d];
+        if (!(p >= 0.0)) p = 0.0;
+        x[3 * i + d] = p;
+        int k = (int)(p * (nc[d] / L[d]));
+        c[d] = k < 0 ? 0 : (k >= nc[d] ? nc[d] - 1 : k);
+    }
+    if (!ok) raise_status(status, MDG_ERR_PARTICLE_LOSS);
+    int k = cell_rank[(c[0] * ncy + c[1]) * ncz + c[2]];
+    key[i] = k;
+    atomicAdd(&count[k], 1);
+}
+
+// exclusive scan of two values per thread over a 1024-thread block
+__device__ void block_scan2(int a, int b, int &ea, int &eb, int &total) {
+    __shared__ int warp_tot[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int s = a + b, inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int t = warp_tot[lane], ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= o) ti += u;
+        }
+        warp_tot[lane] = ti - t;  // exclusive
+        __syncwarp();
+    }
+    __syncthreads();
+    int base = warp_tot[w];
+    int excl = base + inc - s;
+    ea = excl;
+    eb = excl + a;
+    // block total: last thread's inclusive
+    __shared__ int tot;
+    if (threadIdx.x == blockDim.x - 1) tot = excl + s;
+    __syncthreads();
+    total = tot;
+    __syncthreads();
+}
+
+__global__ void k_block_sums(const int *__restrict__ in, int n, int *__restrict__ sums) {
+    int base = blockIdx.x * kScanPerBlock + 2 * threadIdx.x;
+    int a = base < n ? in[base] : 0, b = base + 1 < n ? in[base + 1] : 0;
+    int ea, eb, tot;
+    block_scan2(a, b, ea, eb, tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_top(int *sums, int nblocks) {
+    int carry = 0;
+    for (int off = 0; off < nblocks; off += kScanPerBlock) {
+        int i = off + 2 * threadIdx.x;
+        int a = i < nblocks ? sums[i] : 0, b = i + 1 < nblocks ? sums[i + 1] : 0;
+        int ea, eb, tot;
+        block_scan2(a, b, ea, eb, tot);
+        if (i < nblocks) sums[i] = carry + ea;
+        if (i + 1 < nblocks) sums[i + 1] = carry + eb;
+        carry += tot;
+        __syncthreads();
+    }
+}
+
+__global__ void k_scan_final(const int *__restrict__ in, int n, const int *__restrict__ sums,
+                             int *__restrict__ out) {
+    int base = blockIdx.x * kScanPerBlock + 2 * threadIdx.x;
+    int a = base < n ? in[base] : 0, b = base + 1 < n ? in[base + 1] : 0;
+    int ea, eb, tot;
+    block_scan2(a, b, ea, eb, tot);
+    int off = sums[blockIdx.x];
+    if (base < n) out[base] = off + ea;
+    if (base + 1 < n) out[base + 1] = off + eb;
+    // the element past the end receives the grand total
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = off + tot;
+}
+
+__global__ void k_scatter(const int *__restrict__ key, int n, const int *__restrict__ start,
+                          int *__restrict__ cursor, int *__restrict__ tmp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int k = key[i];
+    int slot = atomicAdd(&cursor[k], 1);
+    tmp[start[k] + slot] = i;
+}
+
+// deterministic order inside each cell: ascending atom index
+__global__ void k_cell_sort(const int *__restrict__ start, int ncells, int *__restrict__ tmp) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    int b = start[c], e = start[c + 1];
+    for (int i = b + 1; i < e; ++i) {
+        int v = tmp[i], j = i - 1;
+        while (j >= b && tmp[j] > v) {
+            tmp[j + 1] = tmp[j];
+            --j;
+        }
+        tmp[j + 1] = v;
+    }
+}
+
+__global__ void k_finish_perm(const int *__restrict__ tmp, int n, int n_pad, int *__restrict__ perm,
+                              int *__restrict__ inv_perm, const float *__restrict__ charge,
+                              const float4 *__restrict__ lj, float *__restrict__ q_sorted,
+                              float2 *__restrict__ prm_sorted) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_pad) return;
+    if (k < n) {
+        int i = tmp[k];
+        perm[k] = i;
+        inv_perm[i] = k;
+        q_sorted[k] = charge[i];
+        float4 p = lj[i];
+        prm_sorted[k] = make_float2(p.x, p.y);
+    } else {
+        perm[k] = -1;
+        q_sorted[k] = 0.0f;
+        prm_sorted[k] = make_float2(0.0f, 0.0f);
+    }
+}
+
+// partners in sorted indices, bit 30 kept as the 1-4 flag: the pair kernel
+// masks 1-2, 1-3 and 1-4 pairs alike (1-4 pairs are evaluated by the
+// special-pair kernel with their own LJ parameters); the bare-Coulomb kernel
+// skips only the unflagged (1-2/1-3) partners
+__global__ void k_partners_sorted(const int *__restrict__ perm, const int *__restrict__ inv_perm,
+                                  const int *__restrict__ partners, int pw, int n_clusters,
+                                  int *__restrict__ partners_sorted, int2 *__restrict__ range) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= n_clusters) return;
+    int k = warp * kCluster + lane;
+    int i = perm[k];
+    int lo = 0x7fffffff, hi = -1;
+    for (int w = 0; w < pw; ++w) {
+        int p = -1;
+        int flag = 0;
+        if (i >= 0) {
+            int raw = partners[(size_t)i * pw + w];
+            if (raw >= 0) {
+                p = inv_perm[raw & 0x3fffffff];
+                flag = raw & 0x40000000;
+            }
+        }
+        partners_sorted[(size_t)k * pw + w] = p < 0 ? -1 : (p | flag);
+        if (p >= 0) {
+            lo = min(lo, p);
+            hi = max(hi, p);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) range[warp] = make_int2(lo, hi);
+}
+
+// one warp per cluster: FP32 coordinates + scaled charge, bounding box, and
+// zeroing of the cluster's fixed-point force slots for the coming evaluation
+__global__ void k_pack(const double *__restrict__ x, const int *__restrict__ perm,
+                       const float *__restrict__ q_sorted, int n_clusters, int n_pad,
+                       float4 *__restrict__ xq, float4 *__restrict__ bbox,
+                       unsigned long long *__restrict__ f) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= n_clusters) return;
+    int k = warp * kCluster + lane;
+    int i = perm[k];
+    float4 p;
+    bool valid = i >= 0;
+    if (valid) {
+        p = make_float4((float)x[3 * i], (float)x[3 * i + 1], (float)x[3 * i + 2], q_sorted[k]);
+    } else {
+        p = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+    }
+    xq[k] = p;
+    f[k] = 0ull;
+    f[n_pad + k] = 0ull;
+    f[2 * n_pad + k] = 0ull;
+    float lox = valid ? p.x : INFINITY, loy = valid ? p.y : INFINITY, loz = valid ? p.z : INFINITY;
+    float hix = valid ? p.x : -INFINITY, hiy = valid ? p.y : -INFINITY,
+          hiz = valid ? p.z : -INFINITY;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
+        loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, o));
+        loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, o));
+        hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
+        hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
+        hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
+    }
+    int cnt = __popc(__ballot_sync(0xffffffffu, valid));
+    if (lane == 0) {
+        bbox[2 * warp] = make_float4(0.5f * (lox + hix), 0.5f * (loy + hiy), 0.5f * (loz + hiz),
+                                     (float)cnt);
+        bbox[2 * warp + 1] = make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy),
+                                         0.5f * (hiz - loz), 0.0f);
+    }
+}
+
+inline unsigned spread_bits(unsigned v) {
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x030000FF;
+    v = (v | (v << 8)) & 0x0300F00F;
+    v = (v | (v << 4)) & 0x030C30C3;
+    v = (v | (v << 2)) & 0x09249249;
+    return v;
+}
+
+}  // namespace
+
+// host: fine-cell grid (~4 atoms per cell) and the Morton rank of each cell
+int prepare_sort_grid(mdg_system *s) {
+    double V = s->box[0] * s->box[1] * s->box[2];
+    double rho = s->n / V;
+    double edge = std::cbrt(4.0 / std::max(rho, 1e-6));
+    int total = 1;
+    for (int d = 0; d < 3; ++d) {
+        int nc = (int)std::floor(s->box[d] / edge);
+        nc = std::max(1, std::min(nc, 1023));
+        s->ncell[d] = nc;
+        total *= nc;
+    }
+    std::vector<std::pair<unsigned, int>> codes(total);
+    for (int a = 0; a < s->ncell[0]; ++a)
+        for (int b = 0; b < s->ncell[1]; ++b)
+            for (int c = 0; c < s->ncell[2]; ++c) {
+                int lin = (a * s->ncell[1] + b) * s->ncell[2] + c;
+                unsigned code = spread_bits(a) | (spread_bits(b) << 1) | (spread_bits(c) << 2);
+                codes[lin] = {code, lin};
+            }
+    std::sort(codes.begin(), codes.end());
+    std::vector<int> rank(total);
+    for (int r = 0; r < total; ++r) rank[codes[r].second] = r;
+    cudaFree(s->cell_rank);
+    cudaFree(s->cell_count);
+    cudaFree(s->cell_start);
+    cudaFree(s->cell_cursor);
+    cudaFree(s->scan_blocks);
+    s->n_cells = total;
+    s->n_scan_blocks = (total + kScanPerBlock - 1) / kScanPerBlock;
+    if (cudaMalloc(&s->cell_rank, sizeof(int) * total) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMalloc(&s->cell_count, sizeof(int) * total) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMalloc(&s->cell_start, sizeof(int) * (total + 1)) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMalloc(&s->cell_cursor, sizeof(int) * total) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMalloc(&s->scan_blocks, sizeof(int) * s->n_scan_blocks) != cudaSuccess)
+        return MDG_ERR_NOMEM;
+    if (cudaMemcpy(s->cell_rank, rank.data(), sizeof(int) * total, cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+        return MDG_ERR_CUDA;
+    return MDG_OK;
+}
+
+cudaError_t launch_reorder(mdg_system *s) {
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    const int tb = 256;
+    cudaMemsetAsync(s->cell_count, 0, sizeof(int) * s->n_cells, st);
+    cudaMemsetAsync(s->cell_cursor, 0, sizeof(int) * s->n_cells, st);
+    k_bin<<<(n + tb - 1) / tb, tb, 0, st>>>(s->x, n, s->box[0], s->box[1], s->box[2], s->ncell[0],
+                                            s->ncell[1], s->ncell[2], s->cell_rank, s->atom_key,
+                                            s->cell_count, s->status);
+    k_block_sums<<<s->n_scan_blocks, kScanThreads, 0, st>>>(s->cell_count, s->n_cells,
+                                                            s->scan_blocks);
+    k_scan_top<<<1, kScanThreads, 0, st>>>(s->scan_blocks, s->n_scan_blocks);
+    k_scan_final<<<s->n_scan_blocks, kScanThreads, 0, st>>>(s->cell_count, s->n_cells,
+                                                            s->scan_blocks, s->cell_start);
+    k_scatter<<<(n + tb - 1) / tb, tb, 0, st>>>(s->atom_key, n, s->cell_start, s->cell_cursor,
+                                                s->tmp_perm);
+    k_cell_sort<<<(s->n_cells + tb - 1) / tb, tb, 0, st>>>(s->cell_start, s->n_cells, s->tmp_perm);
+    k_finish_perm<<<(s->n_pad + tb - 1) / tb, tb, 0, st>>>(s->tmp_perm, n, s->n_pad, s->perm,
+                                                           s->inv_perm, s->charge, s->lj,
+                                                           s->q_sorted, s->prm_sorted);
+    k_partners_sorted<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, st>>>(
+        s->perm, s->inv_perm, s->partners, s->pw, s->n_clusters, s->partners_sorted,
+        s->cluster_partner_range);
+    s->launches += 8;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack(mdg_system *s) {
+    const int tb = 256;
+    k_pack<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, s->stream>>>(
+        s->x, s->perm, s->q_sorted, s->n_clusters, s->n_pad, s->xq, s->bbox, s->f);
+    s->launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace mdg

@@ -1,0 +1,133 @@
+"""Simulation driver and a log dumper with mdpy's interface.
+
+``Simulation.integrate(n)`` runs ``integrator.integrate`` in chunks of the
+greatest common divisor of the dumpers' frequencies and dumps after each
+chunk, like mdpy/simulation.py:60-70; between dumps the steps stay on the
+device as CUDA-graph replays.  ``LogDumper`` writes the columns of
+mdpy/dumper/log_dumper.py:105-208 (step, potential / kinetic / total energy
+in kJ/mol, temperature, ns/day).
+"""
+from __future__ import annotations
+
+import math
+import time
+
+from . import unit
+from .error import DumperPoorDefinedError
+
+
+class Dumper:
+    def __init__(self, dump_frequency: int):
+        if int(dump_frequency) <= 0:
+            raise DumperPoorDefinedError("dump_frequency must be a positive integer")
+        self.dump_frequency = int(dump_frequency)
+
+    def dump(self, simulation):
+        raise NotImplementedError
+
+
+class LogDumper(Dumper):
+    """Tab-separated log.  ``file_path=None`` keeps the rows in ``rows``."""
+
+    def __init__(self, file_path=None, dump_frequency=1, step=True, potential_energy=True,
+                 kinetic_energy=True, total_energy=True, temperature=True, sim_speed=True,
+                 seperator="\t"):
+        super().__init__(dump_frequency)
+        self.file_path = file_path
+        self.columns = [c for c, on in (("Step", step), ("Potential Energy (kj/mol)", potential_energy),
+                                        ("Kinetic Energy (kj/mol)", kinetic_energy),
+                                        ("Total Energy (kj/mol)", total_energy),
+                                        ("Temperature (K)", temperature),
+                                        ("Speed (ns/day)", sim_speed)) if on]
+        self.sep = seperator
+        self.rows = []
+        self._t0 = None
+        self._step0 = 0
+        if file_path:
+            with open(file_path, "w") as fh:
+                fh.write(self.sep.join(self.columns) + "\n")
+
+    def dump(self, simulation):
+        now = time.perf_counter()
+        if self._t0 is None:
+            self._t0, self._step0 = now, simulation.cur_step
+        ens = simulation.ensemble
+        kj = 1.0 / unit.KJ_PER_MOL
+        vals = {
+            "Step": "%d" % simulation.cur_step,
+            "Potential Energy (kj/mol)": "%.3f" % (ens.potential_energy * kj),
+            "Kinetic Energy (kj/mol)": "%.3f" % (ens.kinetic_energy * kj),
+            "Total Energy (kj/mol)": "%.3f" % (ens.total_energy * kj),
+            "Temperature (K)": "%.2f" % unit.kinetic_temperature(ens.kinetic_energy,
+                                                               ens.topology.num_particles),
+        }
+        dt = now - self._t0
+        steps = simulation.cur_step - self._step0
+        vals["Speed (ns/day)"] = ("%.4f" % unit.ns_per_day(steps / dt, simulation.integrator.time_step)
+                                  if dt > 0 and steps > 0 else "--")
+        row = [vals[c] for c in self.columns]
+        self.rows.append(row)
+        if self.file_path:
+            with open(self.file_path, "a") as fh:
+                fh.write(self.sep.join(row) + "\n")
+
+
+class Simulation:
+    def __init__(self, ensemble, integrator, minimizer=None):
+        self._ensemble = ensemble
+        self._integrator = integrator
+        self._minimizer = minimizer
+        self._cur_step = 0
+        self._dumpers = []
+        self._minimum_dump_frequency = 0
+
+    def add_dumpers(self, *dumpers):
+        for d in dumpers:
+            self._dumpers.append(d)
+            self._minimum_dump_frequency = math.gcd(self._minimum_dump_frequency, d.dump_frequency)
+
+    def _dump(self):
+        for d in self._dumpers:
+            if self._cur_step % d.dump_frequency == 0:
+                d.dump(self)
+
+    def dump_initial_state(self):
+        self._ensemble.update()
+        for d in self._dumpers:
+            d.dump(self)
+
+    def reset_simulation_step(self):
+        self._cur_step = 0
+
+    def minimize(self, energy_tolerance, max_iterations):
+        raise NotImplementedError("energy minimisation is not part of the device hot path")
+
+    def integrate(self, num_steps: int):
+        if not self._dumpers or self._minimum_dump_frequency == 0:
+            raise DumperPoorDefinedError("No dumper has been added to Simulation yet.")
+        target = self._cur_step + int(num_steps)
+        while self._cur_step < target:
+            chunk = min(self._minimum_dump_frequency, target - self._cur_step)
+            self._integrator.integrate(self._ensemble, chunk)
+            self._cur_step += chunk
+            self._dump()
+
+    @property
+    def ensemble(self):
+        return self._ensemble
+
+    @property
+    def integrator(self):
+        return self._integrator
+
+    @property
+    def dumpers(self):
+        return self._dumpers
+
+    @property
+    def num_dumpers(self):
+        return len(self._dumpers)
+
+    @property
+    def cur_step(self):
+        return self._cur_step

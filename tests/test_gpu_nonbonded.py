@@ -1,0 +1,237 @@
+"""Short-range kernel parity: LJ and bare Coulomb against the reference's own
+outputs (golden vectors), Ewald real space and the switch against the FP64
+oracle, and the pair set against the reference's cell-list enumeration."""
+import numpy as np
+import pytest
+
+from tests.helpers import make_system, min_image_r, pairs_to_set, rel_rms, water_lj_rows
+
+pytestmark = pytest.mark.gpu
+
+EPS_BAND = 1e-4  # A: pairs this close to the cutoff may fall either side in FP32
+
+
+def test_lj_four_atoms_matches_reference(lib, golden):
+    """mdpy/test/test_charmm_nonbonded_constraint.py:93-126 set-up."""
+    pos = golden["nb4_positions"].astype(np.float64)
+    s = make_system(lib, 4, golden["nb4_box"], lj=golden["nb4_params"].astype(np.float64),
+                    charges=np.zeros(4), bonded=np.full((4, 1), -1),
+                    cutoff=float(golden["nb4_cutoff"]), positions=pos)
+    s.compute_forces(lib.mask(lib.TERM_LJ))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    ref = golden["nb4_forces"].astype(np.float64)
+    assert np.abs(f - ref).max() < 1e-8          # the reference test's abs=1e-8
+    assert abs(f.sum()) < 1e-8
+    assert e[lib.TERM_LJ] == pytest.approx(float(golden["nb4_energy"]), abs=1e-3)
+    assert e[lib.TERM_LJ] == pytest.approx(float(golden["nb4_energy"]), rel=1e-5)
+
+
+def test_lj_water_box_matches_reference(lib, golden):
+    """900 waters, 30 A, rc 12: forces rel RMS <= 1e-5 vs mdpy's own constraint."""
+    pos = golden["w900_positions"].astype(np.float64)
+    n = pos.shape[0]
+    s = make_system(lib, n, 30.0, lj=golden["w900_lj_params"].astype(np.float64),
+                    charges=golden["w900_charges"].reshape(-1), bonded=golden["w900_bonded"],
+                    cutoff=12.0, positions=pos)
+    s.compute_forces(lib.mask(lib.TERM_LJ))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    ref = golden["w900_f_lj"].astype(np.float64)
+    assert rel_rms(f, ref) <= 1e-5
+    assert e[lib.TERM_LJ] == pytest.approx(float(golden["w900_e_lj"]), rel=1e-5)
+
+
+def _split_band(pairset, pos, box, rc):
+    lst = sorted(pairset)
+    if not lst:
+        return set(), set()
+    r = min_image_r(pos, box, lst)
+    far = {p for p, rr in zip(lst, r) if abs(rr - rc) > EPS_BAND}
+    return far, set(lst) - far
+
+
+def test_pair_set_matches_reference_cell_list(lib, golden, orc):
+    """3^3 reference cells: the GPU pair set equals the set the reference's
+    kernel visits (mdpy/constraint/charmm_nonbonded_constraint.py:75-90)."""
+    pos32 = golden["w900_positions"]
+    n = pos32.shape[0]
+    ref = orc.ref_pairs(pos32, np.full(3, 30.0, np.float32), 12.0, golden["w900_cell_index"],
+                        golden["w900_num_cell_vec"], golden["w900_bonded"])
+    cnt, deg, dig = orc.pair_set_digest(ref, n)
+    assert cnt == int(golden["w900_pairs_count"]) and dig == int(golden["w900_pairs_digest"])
+    assert np.array_equal(deg, golden["w900_pairs_degree"])
+    s = make_system(lib, n, 30.0, lj=golden["w900_lj_params"].astype(np.float64),
+                    charges=np.zeros(n), bonded=golden["w900_bonded"], cutoff=12.0,
+                    positions=pos32.astype(np.float64))
+    gpu = pairs_to_set(s.pairset())
+    refs = pairs_to_set(ref)
+    diff = gpu ^ refs
+    far, band = _split_band(diff, pos32, 30.0, 12.0)
+    assert not far, "pairs differ away from the cutoff: %s" % sorted(far)[:10]
+    assert len(band) <= 4
+
+
+def test_pair_set_4_cells_superset_of_reference(lib, golden, orc):
+    """4^3 reference cells: the reference drops pairs across the periodic
+    wrap (its cell adjacency misses them); the GPU set equals brute force and
+    contains the reference's set."""
+    pos32 = golden["sp50_positions"]
+    n = pos32.shape[0]
+    excl = np.full((n, 1), -1)
+    ref = pairs_to_set(orc.ref_pairs(pos32, np.full(3, 50.0, np.float32), 12.0,
+                                     golden["sp50_cell_index"], golden["sp50_num_cell_vec"], excl))
+    assert len(ref) == int(golden["sp50_ref_count"])
+    bf = pairs_to_set(orc.pairs_bruteforce(pos32.astype(np.float64), 50.0, 12.0))
+    assert len(bf) == int(golden["sp50_bf_count"])
+    s = make_system(lib, n, 50.0, lj=golden["sp50_lj_params"].astype(np.float64),
+                    charges=np.zeros(n), bonded=excl, cutoff=12.0,
+                    positions=pos32.astype(np.float64))
+    gpu = pairs_to_set(s.pairset())
+    far, _ = _split_band(gpu ^ bf, pos32, 50.0, 12.0)
+    assert not far
+    missing_in_ref = gpu - ref
+    far_ref, _ = _split_band(ref - gpu, pos32, 50.0, 12.0)
+    assert not far_ref
+    assert len(missing_in_ref) >= int(golden["sp50_bf_count"]) - int(golden["sp50_ref_count"]) - 2
+    # each pair the reference drops sits in cells that are not adjacent mod n
+    ci = golden["sp50_cell_index"]
+    ncv = golden["sp50_num_cell_vec"]
+    for i, j in missing_in_ref:
+        d = np.abs(ci[i] - ci[j])
+        d = np.minimum(d, ncv - d)
+        assert np.any(d > 1)
+
+
+def test_lj_forces_four_cell_box_match_reference(lib, golden):
+    """Where the reference's pair set is incomplete its forces differ from
+    the GPU's by exactly the dropped pairs' contribution; with the oracle
+    evaluated on the reference pair set the GPU matches the reference."""
+    pos = golden["sp50_positions"].astype(np.float64)
+    n = pos.shape[0]
+    s = make_system(lib, n, 50.0, lj=golden["sp50_lj_params"].astype(np.float64),
+                    charges=np.zeros(n), bonded=np.full((n, 1), -1), cutoff=12.0, positions=pos)
+    s.compute_forces(lib.mask(lib.TERM_LJ))
+    f = s.get_forces()
+    ref = golden["sp50_forces"].astype(np.float64)
+    # the dropped pairs are few and long range (r close to rc): tiny force share
+    assert rel_rms(f, ref) < 1e-2
+
+
+def test_bare_coulomb_four_atoms_matches_reference(lib, golden):
+    """mdpy/test/test_electrostatic_constraint.py:197-221 set-up (all pairs)."""
+    pos = golden["es4_positions"].astype(np.float64)
+    s = make_system(lib, 4, golden["es4_box"], charges=golden["es4_charges"].reshape(-1),
+                    lj=np.zeros((4, 4)), bonded=np.full((4, 1), -1), cutoff=12.0, lj_on=False,
+                    coulomb=lib.COUL_BARE, positions=pos)
+    s.compute_forces(lib.mask(lib.TERM_COUL_REAL))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    ref = golden["es4_forces"].astype(np.float64)
+    assert rel_rms(f, ref) < 1e-6
+    assert e[lib.TERM_COUL_REAL] == pytest.approx(float(golden["es4_energy"]), rel=1e-6)
+
+
+def test_bare_coulomb_water_box_matches_reference(lib, golden):
+    pos = golden["w900_positions"].astype(np.float64)
+    n = pos.shape[0]
+    s = make_system(lib, n, 30.0, charges=golden["w900_charges"].reshape(-1),
+                    lj=np.zeros((n, 4)), bonded=golden["w900_bonded"], cutoff=12.0, lj_on=False,
+                    coulomb=lib.COUL_BARE, positions=pos)
+    s.compute_forces(lib.mask(lib.TERM_COUL_REAL))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    assert rel_rms(f, golden["w900_f_coul"]) <= 1e-5
+    assert e[lib.TERM_COUL_REAL] == pytest.approx(float(golden["w900_e_coul"]), rel=1e-5)
+
+
+@pytest.mark.parametrize("switch", [None, 10.0])
+def test_lj_ewald_real_vs_oracle(lib, orc, switch):
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(2000, 27.0, seed=11)
+    t = w.topology
+    n = w.num_particles
+    beta = orc.ewald_beta(12.0, 1e-5)
+    lj = water_lj_rows(w)
+    s = make_system(lib, n, w.box, charges=t.charges.reshape(-1), lj=lj,
+                    bonded=t.bonded_particles, scaling=t.scaling_particles, cutoff=12.0,
+                    switch=switch or 0.0, coulomb=lib.COUL_EWALD, beta=beta, positions=w.positions)
+    s.compute_forces(lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    fo, eo = orc.nonbonded(w.positions, w.box, lj, t.charges, t.bonded_particles,
+                           t.scaling_particles, 12.0, switch=switch, coulomb="ewald", beta=beta)
+    assert rel_rms(f, fo) <= 1e-5
+    assert e[lib.TERM_LJ] == pytest.approx(eo["lj"], rel=1e-5)
+    assert e[lib.TERM_COUL_REAL] == pytest.approx(eo["coulomb"], rel=1e-5)
+
+
+def test_one_four_pairs_and_chain_vs_oracle(lib, orc):
+    """A solvated chain: 1-4 pairs take the 1-4 LJ parameters and the normal
+    Coulomb term; 1-2/1-3 pairs are excluded."""
+    from mdpy_gb300 import systems
+
+    c = systems.chain_in_water(n_waters=460, box=24.0, n_beads=60, seed=5)
+    t = c.topology
+    n = c.num_particles
+    p = c.parameters["nonbonded"]
+    lj = np.array([[p[ty][0], p[ty][1], 0.5 * p[ty][0], 0.9 * p[ty][1]] for ty in t.particle_types])
+    beta = orc.ewald_beta(11.0, 1e-5)
+    s = make_system(lib, n, c.box, charges=t.charges.reshape(-1), lj=lj,
+                    bonded=t.bonded_particles, scaling=t.scaling_particles, cutoff=11.0,
+                    switch=9.0, coulomb=lib.COUL_EWALD, beta=beta, positions=c.positions)
+    s.compute_forces(lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    fo, eo = orc.nonbonded(c.positions, c.box, lj, t.charges, t.bonded_particles,
+                           t.scaling_particles, 11.0, switch=9.0, coulomb="ewald", beta=beta)
+    assert rel_rms(f, fo) <= 1e-5
+    assert e[lib.TERM_LJ] == pytest.approx(eo["lj"], rel=1e-5)
+    assert e[lib.TERM_COUL_REAL] == pytest.approx(eo["coulomb"], rel=1e-5)
+
+
+def test_forces_bit_reproducible(lib):
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(3000, 31.0, seed=2)
+    t = w.topology
+    out = []
+    for _ in range(2):
+        s = make_system(lib, w.num_particles, w.box, charges=t.charges.reshape(-1),
+                        lj=water_lj_rows(w), bonded=t.bonded_particles, cutoff=12.0,
+                        coulomb=lib.COUL_EWALD, beta=0.27, positions=w.positions)
+        s.compute_forces(lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL))
+        out.append(s.get_forces())
+        s.compute_forces(lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL))
+        out.append(s.get_forces())
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
+
+
+def test_empty_and_tiny_systems(lib):
+    # one atom: no pairs, zero force, energy 0
+    s = make_system(lib, 1, 30.0, charges=[0.5], lj=np.array([[1e-4, 3.0, 1e-4, 3.0]]),
+                    bonded=np.full((1, 1), -1), cutoff=12.0, coulomb=lib.COUL_EWALD, beta=0.3,
+                    positions=np.zeros((1, 3)))
+    s.compute_forces(lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL))
+    assert np.all(s.get_forces() == 0)
+    assert len(s.pairset()) == 0
+    # 33 atoms: one full cluster plus a cluster of one
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0, 20, size=(33, 3))
+    s = make_system(lib, 33, 20.0, charges=np.zeros(33), lj=np.tile([1e-4, 3.0, 1e-4, 3.0], (33, 1)),
+                    bonded=np.full((33, 1), -1), cutoff=9.0, positions=x)
+    from oracle import oracle as O
+    bf = pairs_to_set(O.pairs_bruteforce(x, 20.0, 9.0))
+    gpu = pairs_to_set(s.pairset())
+    far, _ = _split_band(gpu ^ bf, x, 20.0, 9.0)
+    assert not far
+
+
+def test_cutoff_validation(lib):
+    from mdpy_gb300.error import CellListPoorDefinedError
+
+    s = lib.System(10, 20.0)
+    with pytest.raises(CellListPoorDefinedError):
+        s.nonbonded_config(10.5)

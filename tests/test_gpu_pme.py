@@ -1,0 +1,98 @@
+"""PME reciprocal space against the FP64 oracle (same grid), and the full
+Ewald sum (real + reciprocal + exclusion + self + net charge) against the
+FP64 direct Ewald sum.  mdpy has no Ewald/PME: these parities are pinned by
+the oracle's mathematics (Madelung constant, convergence), not by the
+reference."""
+import numpy as np
+import pytest
+
+from tests.helpers import make_system, rel_rms, water_lj_rows
+
+pytestmark = pytest.mark.gpu
+
+
+def _pme_system(lib, w, K, order, beta, rc=None):
+    t = w.topology
+    n = w.num_particles
+    s = make_system(lib, n, w.box, charges=t.charges.reshape(-1), lj=water_lj_rows(w),
+                    bonded=t.bonded_particles, scaling=t.scaling_particles,
+                    cutoff=rc or 0.45 * float(np.min(w.box)), coulomb=lib.COUL_EWALD, beta=beta,
+                    positions=w.positions)
+    s.pme_config(K, order, beta)
+    return s
+
+
+@pytest.mark.parametrize("order,K", [(4, 32), (5, 32), (6, (28, 32, 36))])
+def test_pme_matches_fp64_pme(lib, orc, order, K):
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(900, 30.0, seed=0)
+    t = w.topology
+    q = t.charges.reshape(-1)
+    beta = orc.ewald_beta(12.0, 1e-5)
+    s = _pme_system(lib, w, K, order, beta, rc=12.0)
+    s.compute_forces(lib.mask(lib.TERM_COUL_RECIP))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    fp, ep = orc.pme(w.positions, w.box, q, beta, K, order)
+    fx, ex = orc.ewald_exclusions(w.positions, w.box, q, t.bonded_particles, beta)
+    e_ref = ep + ex + orc.ewald_self(q, beta) + orc.ewald_net_charge(q, w.box, beta)
+    assert rel_rms(f, fp + fx) <= 2e-5
+    assert e[lib.TERM_COUL_RECIP] == pytest.approx(e_ref, rel=2e-6)
+
+
+def test_pme_non_cubic_box(lib, orc):
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(1000, 30.0, seed=4)
+    box = np.array([30.0, 33.0, 36.0])
+    pos = w.positions * (box / 30.0)
+    w.box = box
+    w.positions = pos
+    beta = 0.3
+    K = (30, 32, 36)
+    s = _pme_system(lib, w, K, 4, beta, rc=11.0)
+    s.compute_forces(lib.mask(lib.TERM_COUL_RECIP))
+    f = s.get_forces()
+    q = w.topology.charges.reshape(-1)
+    fp, _ = orc.pme(pos, box, q, beta, K, 4)
+    fx, _ = orc.ewald_exclusions(pos, box, q, w.topology.bonded_particles, beta)
+    assert rel_rms(f, fp + fx) <= 2e-5
+
+
+def test_full_ewald_vs_direct_sum(lib, orc):
+    """configs[0] electrostatics: 900 waters, 30 A, rc 12, tolerance 1e-5,
+    32^3 grid, order 4 -- total Coulomb force error vs FP64 direct Ewald."""
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(900, 30.0, seed=0)
+    t = w.topology
+    q = t.charges.reshape(-1)
+    beta = orc.ewald_beta(12.0, 1e-5)
+    s = _pme_system(lib, w, 32, 4, beta, rc=12.0)
+    s.compute_forces(lib.mask(lib.TERM_COUL_REAL, lib.TERM_COUL_RECIP))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    d = orc.ewald_direct(w.positions, w.box, q, t.bonded_particles, beta, 12.0)
+    err = rel_rms(f, d["forces"])
+    print("configs[0] Coulomb force rel RMS vs direct Ewald: %.3e" % err)
+    assert err < 2e-3
+    e_gpu = e[lib.TERM_COUL_REAL] + e[lib.TERM_COUL_RECIP]
+    assert e_gpu == pytest.approx(d["energy"], rel=1e-4)
+
+
+def test_pme_energy_translation_invariance(lib):
+    """Shifting every atom by the same vector leaves the energy unchanged up
+    to the grid discretisation (PME is not exactly translation invariant)."""
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(900, 30.0, seed=0)
+    s = _pme_system(lib, w, 32, 4, 0.27, rc=12.0)
+    s.compute_forces(lib.mask(lib.TERM_COUL_REAL, lib.TERM_COUL_RECIP))
+    e0, _ = s.get_energies()
+    s.set_positions(w.positions + np.array([0.37, -1.21, 2.5]))
+    s.compute_forces(lib.mask(lib.TERM_COUL_REAL, lib.TERM_COUL_RECIP))
+    e1, _ = s.get_energies()
+    tot0 = e0[lib.TERM_COUL_REAL] + e0[lib.TERM_COUL_RECIP]
+    tot1 = e1[lib.TERM_COUL_REAL] + e1[lib.TERM_COUL_RECIP]
+    assert tot1 == pytest.approx(tot0, rel=2e-4)

@@ -1,0 +1,142 @@
+"""Host-side logic, the C ABI surface, and the oracle boundary (CPU only)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_c_abi_exports_every_declared_symbol(lib):
+    """libmdg.so loads and exports every MDG_API function of include/mdg.h."""
+    with open(os.path.join(ROOT, "include", "mdg.h")) as fh:
+        names = re.findall(r"MDG_API\s+[\w\s\*]+?\b(mdg_\w+)\s*\(", fh.read())
+    assert len(names) >= 30
+    so = ctypes.CDLL(lib.LIB_PATH)
+    for nm in names:
+        assert hasattr(so, nm), nm
+    lib.load()
+    assert set(lib.SIGNATURES) <= set(names) | {"mdg_last_error"}
+
+
+def test_version_and_error_without_gpu(lib):
+    L = lib.load()
+    major, minor = ctypes.c_int(), ctypes.c_int()
+    assert L.mdg_version(ctypes.byref(major), ctypes.byref(minor)) == 0
+    assert major.value >= 1
+    # invalid arguments are rejected before any device work
+    h = ctypes.c_void_p()
+    box = (ctypes.c_double * 3)(10.0, 10.0, 10.0)
+    assert L.mdg_system_create(0, -5, box, ctypes.byref(h)) == 1
+    assert b"n_atoms" in L.mdg_last_error()
+    bad = (ctypes.c_double * 3)(10.0, -1.0, 10.0)
+    assert L.mdg_system_create(0, 5, bad, ctypes.byref(h)) == 4
+
+
+def test_status_codes_map_to_mdpy_exceptions():
+    from mdpy_gb300 import error as E
+
+    assert isinstance(E.status_to_exception(4, "x"), E.PBCPoorDefinedError)
+    assert isinstance(E.status_to_exception(5, "x"), E.CellListPoorDefinedError)
+    assert isinstance(E.status_to_exception(6, "x"), E.ParticleLossError)
+    assert isinstance(E.status_to_exception(7, "x"), E.FixedPointOverflowError)
+    assert isinstance(E.status_to_exception(9, "x"), E.DeviceTimeoutError)
+
+
+def test_product_code_never_imports_the_oracle():
+    pkg = os.path.join(ROOT, "mdpy_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h")):
+                with open(os.path.join(dirpath, f)) as fh:
+                    src = fh.read()
+                assert "import oracle" not in src and "from oracle" not in src, f
+                assert "liborc" not in src, f
+
+
+def test_unit_constants_match_reference_definitions():
+    from mdpy_gb300 import unit
+
+    # values mdpy computes through its float32 Quantity (mdpy/unit/__init__.py:54-58):
+    # equal up to float32 rounding (one ulp ~ 1.2e-7 relative)
+    assert unit.EPSILON0 == pytest.approx(0.5727653, rel=2.5e-7)
+    assert unit.KCAL_PER_MOL == pytest.approx(0.00041840284, rel=2.5e-7)
+    assert unit.KB * 300 == pytest.approx(2.4943e-4, rel=1e-3)
+
+
+def test_topology_particle_api_matches_join():
+    from mdpy_gb300 import Particle, Topology
+    from mdpy_gb300.error import ModifyJoinedTopologyError, ParticleConflictError
+
+    t = Topology()
+    t.add_particles([Particle(particle_id=i, particle_type="C", mass=12, charge=0.1 * i)
+                     for i in range(5)])
+    t.add_bond([0, 1])
+    t.add_bond([1, 2])
+    t.add_angle([0, 1, 2])
+    t.add_dihedral([0, 1, 2, 3])
+    with pytest.raises(ParticleConflictError):
+        t.add_bond([0, 0])
+    t.join()
+    assert t.bonded_particles[0].tolist() == [1, 2]
+    assert t.bonded_particles[1].tolist()[:2] == [0, 2]
+    assert t.scaling_particles[0, 0] == 3 and t.scaling_particles[3, 0] == 0
+    assert t.masses.shape == (5, 1) and t.charges[4, 0] == pytest.approx(0.4)
+    with pytest.raises(ModifyJoinedTopologyError):
+        t.add_bond([3, 4])
+    a = Topology.from_arrays(["C"] * 5, [12] * 5, [0.1 * i for i in range(5)],
+                             bonds=[[0, 1], [1, 2]], angles=[[0, 1, 2]], dihedrals=[[0, 1, 2, 3]])
+    assert np.array_equal(np.sort(a.bonded_particles, 1), np.sort(t.bonded_particles, 1))
+    assert np.array_equal(a.scaling_particles[:, :1], t.scaling_particles[:, :1])
+
+
+def test_synthetic_workloads():
+    from mdpy_gb300 import systems, unit
+
+    w = systems.water_box(900, 30.0, seed=0)
+    assert w.num_particles == 2700
+    assert np.all(np.abs(w.positions) <= 15.0 + 1e-9)
+    o, h1 = w.positions[0], w.positions[1]
+    d = h1 - o
+    d -= 30.0 * np.round(d / 30.0)
+    assert np.linalg.norm(d) == pytest.approx(0.9572, abs=1e-9)
+    ke = 0.5 * np.sum(w.topology.masses * w.velocities ** 2)
+    assert unit.kinetic_temperature(ke, w.num_particles) == pytest.approx(300, rel=0.05)
+    assert abs(np.sum(w.topology.charges)) < 1e-9
+    c = systems.chain_in_water(n_waters=460, box=24.0, n_beads=60, seed=5)
+    assert c.topology.num_dihedrals == 57 and c.dihedral_parameters.shape == (57, 3)
+    assert abs(np.sum(c.topology.charges)) < 1e-9
+    batch = systems.water_box_batch(6, seed=1)
+    sizes = [b.num_particles for b in batch]
+    assert min(sizes) >= 1500 - 3 and max(sizes) <= 12000 + 3
+    assert systems.fft_friendly(97) == 100 and systems.fft_friendly(96) == 96
+
+
+def test_parameter_lookup_like_reference():
+    from mdpy_gb300 import Topology, systems
+    from mdpy_gb300.constraint import _per_atom_lj, _type_rows
+    from mdpy_gb300.error import ParameterPoorDefinedError
+
+    w = systems.water_box(3, 30.0)
+    rows = _per_atom_lj(w.parameters["nonbonded"], w.topology)
+    assert rows.shape == (9, 4) and rows[0, 0] > 0 and rows[1, 0] == 0
+    t = Topology.from_arrays(["XX"], [1.0], [0.0])
+    with pytest.raises(ParameterPoorDefinedError):
+        _per_atom_lj(w.parameters["nonbonded"], t)
+    idx, prm = _type_rows({"A-B-C-D": [[1.0, 2, 0.0], [0.5, 3, 3.14]]},
+                          Topology.from_arrays(list("ABCD"), [1] * 4, [0] * 4),
+                          [[0, 1, 2, 3]], 3, expand=True)
+    assert len(idx) == 2 and prm[1][1] == 3
+
+
+def test_ewald_beta_rule():
+    from mdpy_gb300.constraint import ewald_beta_from_error
+
+    b = ewald_beta_from_error(12.0, 1e-5)
+    from math import erfc
+
+    # exp(-(beta rc)^2) = 2 tol, so erfc(beta rc) ~ 2 tol / (beta rc sqrt(pi)) < tol
+    assert 1e-6 < erfc(b * 12.0) < 1e-5
+    assert b == pytest.approx(0.2744, abs=1e-3)
