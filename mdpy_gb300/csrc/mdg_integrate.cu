@@ -144,7 +144,9 @@ __global__ void k_forces_out(const unsigned long long *__restrict__ f,
     out[3 * i + 2] = fget(f, 2 * n_pad + k);
 }
 
-// reference convention: x - L round(x/L) (mdpy/utils/pbc.py:28-36)
+// mdpy's wrap_positions (mdpy/utils/pbc.py:28-36): x - L round(x * inv) with
+// inv = float32(1/L) as mdpy stores pbc_inv (mdpy/core/state.py:53-54), so an
+// exact half-box coordinate lands on the side mdpy puts it
 __global__ void k_positions_out(const double *__restrict__ x, int n, double Lx, double Ly,
                                 double Lz, double *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -153,7 +155,8 @@ __global__ void k_positions_out(const double *__restrict__ x, int n, double Lx, 
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double p = x[3 * i + d];
-        out[3 * i + d] = p - L[d] * rint(p / L[d]);
+        const double inv32 = (double)(float)(1.0 / L[d]);
+        out[3 * i + d] = p - L[d] * rint(p * inv32);
     }
 }
 

@@ -67,14 +67,17 @@ struct PmeArgs {
     unsigned long long *f;
 };
 
+// grid coordinate u = x K / L wrapped into [0, K) with fmodf (exact), so the
+// first stencil point g0 is a valid index for any finite or non-finite x
 template <int P>
 __device__ __forceinline__ void frac(float x, float kl, int K, int &g0, float &w) {
-    float u = x * kl;
-    u -= (float)K * floorf(u / (float)K);
-    int m = (int)floorf(u);
+    const float Kf = (float)K;
+    float u = fmodf(x * kl, Kf);
+    if (u < 0.f) u += Kf;
+    if (!(u >= 0.f && u < Kf)) u = 0.f;  // NaN, or -tiny + K rounding to K
+    int m = (int)u;
+    if (m > K - 1) m = K - 1;
     w = u - (float)m;
-    if (m >= K) m -= K;
-    if (m < 0) m += K;
     g0 = m - P + 1;
     if (g0 < 0) g0 += K;
 }

@@ -427,6 +427,10 @@ def kinetic_energy(v, masses):
 
 
 def wrap_positions(positions, box):
-    """Reference convention: x - L round(x/L) (mdpy/utils/pbc.py:28-36)."""
+    """mdpy's wrap_positions (mdpy/utils/pbc.py:28-36): x - L round(x inv),
+    with inv the float32 inverse mdpy keeps (State.set_pbc_matrix,
+    mdpy/core/state.py:53-54) -- so exact half-box coordinates wrap to the
+    side mdpy puts them (+L/2 -> -L/2 when float32(1/L) > 1/L)."""
     b = np.broadcast_to(np.asarray(box, float), (3,))
-    return positions - b * np.round(positions / b)
+    inv32 = (1.0 / b).astype(np.float32).astype(np.float64)
+    return positions - b * np.round(np.asarray(positions, dtype=np.float64) * inv32)

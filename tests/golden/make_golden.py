@@ -23,6 +23,8 @@ Cases (every array is the reference's own output unless noted):
 * ``w900_*``  -- 900 waters / 30 A (3^3 reference cells): LJ, Coulomb, bond and
   angle forces/energies, the reference cell list and the digest of the pair set
   its nonbonded kernel visits
+* ``wb900_*`` -- the same waters displaced by N(0, 0.05 A): bond and angle
+  forces/energies away from equilibrium
 * ``sp50_*``  -- 1500 random LJ atoms in a 50 A box (4^3 reference cells): the
   reference LJ forces, its cell list and pair-set digest, and the brute-force
   digest (shows the pairs the reference drops across the periodic wrap)
@@ -200,6 +202,17 @@ def main(ref_root):
                w900_pairs_degree=deg, w900_pairs_digest=np.uint64(dig),
                w900_lj_params=cons["lj"]._parameters_list, w900_bonded=t.bonded_particles,
                w900_charges=t.charges, w900_masses=t.masses)
+
+    # -- bonded terms away from equilibrium (the generated waters sit exactly at
+    #    r0/theta0, where bond/angle forces are only float32 rounding noise)
+    rng = np.random.default_rng(900)
+    pert = (pos32 + rng.normal(0.0, 0.05, size=pos32.shape)).astype(np.float32)
+    ens.state.set_positions(pert)
+    for k in ("bond", "angle"):
+        cons[k].update()
+        out["wb900_f_" + k] = cons[k].forces
+        out["wb900_e_" + k] = np.float64(cons[k].potential_energy)
+    out["wb900_positions"] = ens.state.positions
 
     # -- sparse 50 A box, 4^3 reference cells
     rng = np.random.default_rng(50)

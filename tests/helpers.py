@@ -1,6 +1,11 @@
 """Shared builders for the tests (no GPU work at import time)."""
 import numpy as np
 
+# Tolerance on totals the reference accumulates in float32 over 10^5-10^6
+# terms (its forces are per-atom sums of ~10^3 terms and stay at ~1e-6):
+# the reference's own rounding error in such a total reaches ~1e-4.
+REF_E_TOL = 2e-4
+
 
 def rel_rms(a, b):
     a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
@@ -55,3 +60,25 @@ def min_image_r(pos, box, pairs):
     d = pos[p[:, 1]] - pos[p[:, 0]]
     d -= box * np.round(d / box)
     return np.sqrt((d ** 2).sum(1))
+
+
+def half_box_tie_atoms(pos, box, tol=2e-6):
+    """Atoms of pairs whose separation along some axis lies within ``tol`` of
+    half the box: there the minimum image is a tie that float32 and FP64
+    (or two rounding rules) may break differently.  All pairs, O(N^2)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    box = np.broadcast_to(np.asarray(box, float), (3,))
+    atoms = set()
+    for k in range(3):
+        d = np.abs(pos[None, :, k] - pos[:, None, k])
+        d = np.abs(d - box[k] * np.round(d / box[k]))
+        i, j = np.nonzero(np.abs(d - box[k] / 2) < tol)
+        atoms.update(i.tolist())
+        atoms.update(j.tolist())
+    return np.array(sorted(atoms), dtype=np.int64)
+
+
+def rel_rms_excluding(a, b, drop):
+    keep = np.ones(len(a), dtype=bool)
+    keep[np.asarray(drop, dtype=np.int64)] = False
+    return rel_rms(np.asarray(a)[keep], np.asarray(b)[keep])

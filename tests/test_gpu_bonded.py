@@ -4,7 +4,7 @@ improper energies against the reference, forces against the exact gradient
 import numpy as np
 import pytest
 
-from tests.helpers import make_system, rel_rms
+from tests.helpers import REF_E_TOL, make_system, rel_rms
 
 pytestmark = pytest.mark.gpu
 
@@ -47,7 +47,7 @@ def test_torsions_energy_reference_forces_exact(lib, golden, orc, key, setter, t
 def test_water_bonds_angles_match_reference(lib, golden):
     from mdpy_gb300 import systems
 
-    pos = golden["w900_positions"].astype(np.float64)
+    pos = golden["wb900_positions"].astype(np.float64)
     w = systems.water_box(900, 30.0, seed=0)
     t = w.topology
     kb = np.array([w.parameters["bond"]["OT-HT"]] * t.num_bonds)
@@ -55,12 +55,12 @@ def test_water_bonds_angles_match_reference(lib, golden):
     s = make_system(lib, pos.shape[0], 30.0, positions=pos)
     s.set_bonds(t.bonds, kb)
     s.set_angles(t.angles, ka)
-    for term, key, en in ((lib.TERM_BOND, "w900_f_bond", "w900_e_bond"),
-                          (lib.TERM_ANGLE, "w900_f_angle", "w900_e_angle")):
+    for term, key, en in ((lib.TERM_BOND, "wb900_f_bond", "wb900_e_bond"),
+                          (lib.TERM_ANGLE, "wb900_f_angle", "wb900_e_angle")):
         s.compute_forces(lib.mask(term))
         e, _ = s.get_energies()
         assert rel_rms(s.get_forces(), golden[key]) <= 1e-5
-        assert e[term] == pytest.approx(float(golden[en]), rel=1e-5)
+        assert e[term] == pytest.approx(float(golden[en]), rel=REF_E_TOL)
 
 
 def test_chain_bonded_vs_oracle(lib, orc):
