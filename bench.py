@@ -304,7 +304,10 @@ def main():
     n = s.num_particles
     ens, beta = make_ensemble(s, local)
     sysm = ens.system
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library, the L2 flush and the timing events all
+    # go to it (torch's default stream is the legacy stream, handle 0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sysm.set_stream(stream.cuda_stream)
     integ = LangevinIntegrator(DT_FS, TEMPERATURE, FRICTION, seed=1000 + rank)
     integ._configure(ens)

@@ -136,6 +136,7 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
         CK(e, "pme");
     }
     CK(launch_bonded(s, mask, energy), "bonded");
+    s->evaluated_once = 1;
     return MDG_OK;
 }
 
@@ -949,7 +950,7 @@ MDG_API int mdg_set_graph_mode(mdg_system *s, int mode) {
 MDG_API int mdg_launch_stage(mdg_system *s, int stage, unsigned mask) {
     int rc = check_sys(s);
     if (rc) return rc;
-    if (!s->forces_valid && stage != MDG_STAGE_REORDER && stage != MDG_STAGE_PACK)
+    if (!s->evaluated_once)
         return fail(MDG_ERR_STATE, "evaluate the system once before launching single stages");
     mask &= MDG_MASK_ALL;
     switch (stage) {

@@ -166,15 +166,15 @@ __global__ void __launch_bounds__(256) k_bonded(BdArgs a) {
             addf(a, id.w, -dv * g[3].x, -dv * g[3].y, -dv * g[3].z);
         }
     }
-    __shared__ float s_e[8];
-    e = warp_sum(e);
-    if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = e;
+    __shared__ double s_e[8];
+    const double d = warp_sum_d((double)e);
+    if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = d;
     __syncthreads();
     if (threadIdx.x == 0) {
-        float tot = 0.f;
+        double tot = 0.0;
         for (int w = 0; w < 8; ++w) tot += s_e[w];
         const int term = MDG_TERM_BOND + seg;
-        fix_red((unsigned long long *)&a.energy[term], to_fix(tot));
+        fix_red((unsigned long long *)&a.energy[term], to_fix_d(tot));
     }
 }
 

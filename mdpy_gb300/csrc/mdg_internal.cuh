@@ -150,6 +150,7 @@ struct mdg_system {
     int reorder_interval = 20;
     int steps_since_reorder = 0;
     int forces_valid = 0;
+    int evaluated_once = 0;
     unsigned forces_mask = 0;
     long long launches = 0;
     mdg::Graph graph;                  // chunk of reorder_interval steps

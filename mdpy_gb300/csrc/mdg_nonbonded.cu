@@ -56,6 +56,7 @@ struct NbArgs {
     int n, n_pad, n_clusters;
     float L[3], invL[3];
     float rc, rc2, rs2, sw_inv_den;
+    float beta;
     float beta_p;        // A&S p * beta
     float ewald_exp_c;   // beta^2 log2(e)
     float ewald_fc;      // 2 beta / sqrt(pi)
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
     __shared__ float2 s_jp[kWarps][kRing];
     __shared__ int2 s_jm[kWarps][kRing];
     __shared__ float s_fi[3][kWarps][32];
-    __shared__ float s_e[2][kWarps];
+    __shared__ double s_e[2][kWarps];
 
     const int I = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -98,13 +99,14 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
     const int ilo = I * kCluster;
 
     float fix = 0.f, fiy = 0.f, fiz = 0.f;
-    float acc_lj = 0.f, acc_c = 0.f;
+    double acc_lj = 0.0, acc_c = 0.0;  // per-lane energies: FP32 within a chunk, FP64 across
     unsigned long long n_eval = 0, n_in = 0;
     int jbase = 0, jcount = 0;
 
     // sweep of one 32-entry chunk starting at ring slot `base`
     auto chunk = [&](int base) {
         float fjx = 0.f, fjy = 0.f, fjz = 0.f;
+        float c_lj = 0.f, c_c = 0.f;
 #pragma unroll 4
         for (int t = 0; t < 32; ++t) {
             const int e = (base + ((lane + t) & 31)) & (kRing - 1);
@@ -151,8 +153,13 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
                 const float poly =
                     tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, kAsA5, kAsA4), kAsA3), kAsA2), kAsA1);
                 const float ex = exp2f(-a.ewald_exp_c * r2s);
-                ecl = qq * poly * ex * rinv;
-                fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecl), rinv2, fr);
+                const float ecf = qq * poly * ex * rinv;
+                fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecf), rinv2, fr);
+                // the force keeps the 1.5e-7 approximation in every variant (so a
+                // trajectory does not depend on when energies are reported); the
+                // reported energy uses the library erfc, whose error does not pile
+                // up over 10^6 pairs
+                if (ENERGY) ecl = qq * erfcf(a.beta * r) * rinv;
             }
             fr = inc ? fr : 0.f;
             fix = fmaf(-fr, dx, fix);
@@ -162,8 +169,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
             fjy = fmaf(fr, dy, fjy);
             fjz = fmaf(fr, dz, fjz);
             if (ENERGY) {
-                acc_lj += inc ? elj : 0.f;
-                acc_c += inc ? ecl : 0.f;
+                c_lj += inc ? elj : 0.f;
+                c_c += inc ? ecl : 0.f;
                 n_in += __popc(__ballot_sync(kFull, inc));
             }
             const int src = (lane + 1) & 31;
@@ -180,7 +187,11 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
             fix_red(&a.f[a.n_pad + jk], to_fix(fjy));
             fix_red(&a.f[2 * a.n_pad + jk], to_fix(fjz));
         }
-        n_eval += 32;
+        if (ENERGY) {
+            acc_lj += (double)c_lj;
+            acc_c += (double)c_c;
+        }
+        n_eval += 32 * 32;
         __syncwarp();
     };
 
@@ -313,7 +324,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
     s_fi[1][warp][lane] = fiy;
     s_fi[2][warp][lane] = fiz;
     if (ENERGY) {
-        const float el = warp_sum(acc_lj), ee = warp_sum(acc_c);
+        const double el = warp_sum_d(acc_lj), ee = warp_sum_d(acc_c);
         if (lane == 0) {
             s_e[0][warp] = el;
             s_e[1][warp] = ee;
@@ -336,15 +347,15 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
             fix_red(&a.f[2 * a.n_pad + ik], to_fix(sz));
         }
         if (ENERGY && lane == 0) {
-            float el = 0.f, ee = 0.f;
+            double el = 0.0, ee = 0.0;
             for (int w = 0; w < kWarps; ++w) {
                 el += s_e[0][w];
                 ee += s_e[1][w];
             }
-            if (!(fabsf(el) < kFixLimit && fabsf(ee) < kFixLimit))
+            if (!(fabs(el) < kFixLimit && fabs(ee) < kFixLimit))
                 raise_status(a.status, MDG_ERR_OVERFLOW);
-            fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix(el));
-            fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix(ee));
+            fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix_d(el));
+            fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix_d(ee));
         }
     }
     if (ENERGY && lane == 0) {
@@ -509,27 +520,28 @@ __global__ void k_special(SpArgs a) {
         }
     }
     if (DUMP) return;
-    __shared__ float s_e[3][8];
-    e_lj = warp_sum(e_lj);
-    e_cr = warp_sum(e_cr);
-    e_rec = warp_sum(e_rec);
+    // FP64 block sums: the exclusion term is a sum of O(10^5) terms of either
+    // sign whose total largely cancels the self energy
+    __shared__ double s_e[3][8];
+    const double d_lj = warp_sum_d((double)e_lj), d_cr = warp_sum_d((double)e_cr),
+                 d_rec = warp_sum_d((double)e_rec);
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        s_e[0][w] = e_lj;
-        s_e[1][w] = e_cr;
-        s_e[2][w] = e_rec;
+        s_e[0][w] = d_lj;
+        s_e[1][w] = d_cr;
+        s_e[2][w] = d_rec;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
             a0 += s_e[0][k];
             a1 += s_e[1][k];
             a2 += s_e[2][k];
         }
-        if (a0 != 0.f) fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix(a0));
-        if (a1 != 0.f) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix(a1));
-        if (a2 != 0.f) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_RECIP], to_fix(a2));
+        if (a0 != 0.0) fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix_d(a0));
+        if (a1 != 0.0) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix_d(a1));
+        if (a2 != 0.0) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_RECIP], to_fix_d(a2));
     }
 }
 
@@ -554,6 +566,7 @@ NbArgs make_args(mdg_system *s) {
     a.rs2 = (float)(rs * rs);
     const double den = (double)a.rc2 - rs * rs;
     a.sw_inv_den = den > 0 ? (float)(1.0 / (den * den * den)) : 0.f;
+    a.beta = (float)s->beta;
     a.beta_p = kAsP * (float)s->beta;
     a.ewald_exp_c = (float)(s->beta * s->beta * 1.4426950408889634);
     a.ewald_fc = (float)(2.0 * s->beta / 1.7724538509055159);

@@ -139,14 +139,14 @@ __global__ void __launch_bounds__(256) k_convolve(float2 *__restrict__ gc,
         gc[i] = make_float2(c.x * g, c.y * g);
     }
     if (ENERGY) {
-        __shared__ float s_e[8];
-        e = warp_sum(e);
-        if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = e;
+        __shared__ double s_e[8];
+        const double d = warp_sum_d((double)e);
+        if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = d;
         __syncthreads();
         if (threadIdx.x == 0) {
-            float t = 0.f;
+            double t = 0.0;
             for (int w = 0; w < 8; ++w) t += s_e[w];
-            fix_red((unsigned long long *)&energy[MDG_TERM_COUL_RECIP], to_fix(t));
+            fix_red((unsigned long long *)&energy[MDG_TERM_COUL_RECIP], to_fix_d(t));
         }
     }
 }

@@ -39,8 +39,8 @@ class CellListView:
 
     def __init__(self, state, cutoff_radius=12.0):
         self._state = state
-        self._cutoff_radius = 0.0
-        self.set_cutoff_radius(cutoff_radius)
+        # mdpy's default 12 A, reduced for boxes under 24 A instead of raising
+        self._cutoff_radius = float(min(cutoff_radius, np.min(state.box) / 2.0))
 
     def set_cutoff_radius(self, cutoff_radius):
         rc = float(unit.check_quantity_value(cutoff_radius, "angstrom"))

@@ -25,7 +25,7 @@ Cases (every array is the reference's own output unless noted):
   its nonbonded kernel visits
 * ``wb900_*`` -- the same waters displaced by N(0, 0.05 A): bond and angle
   forces/energies away from equilibrium
-* ``sp50_*``  -- 1500 random LJ atoms in a 50 A box (4^3 reference cells): the
+* ``sp50_*``  -- 1500 random LJ atoms (2.8 A hard core) in a 50 A box (4^3 reference cells): the
   reference LJ forces, its cell list and pair-set digest, and the brute-force
   digest (shows the pairs the reference drops across the periodic wrap)
 * ``v81_*``   -- one VerletIntegrator step of 27 waters in a 25 A box
@@ -215,9 +215,20 @@ def main(ref_root):
     out["wb900_positions"] = ens.state.positions
 
     # -- sparse 50 A box, 4^3 reference cells
+    # random sequential addition with a 2.8 A hard core: uniform-random points
+    # put pairs far inside the LJ core (forces ~1e11, beyond any physical state)
     rng = np.random.default_rng(50)
     n = 1500
-    sp = (rng.uniform(-25, 25, size=(n, 3))).astype(np.float32)
+    pts = []
+    while len(pts) < n:
+        c = rng.uniform(-25, 25, size=3)
+        if pts:
+            d = np.asarray(pts) - c
+            d -= 50.0 * np.round(d / 50.0)
+            if np.min(np.einsum("ij,ij->i", d, d)) < 2.8 ** 2:
+                continue
+        pts.append(c)
+    sp = np.asarray(pts).astype(np.float32)
     t = Topology()
     t.add_particles([Particle(particle_id=i, particle_type="OT", particle_name="OT",
                               molecule_type="X", mass=16.0, charge=0.0) for i in range(n)])

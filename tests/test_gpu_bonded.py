@@ -79,7 +79,7 @@ def test_chain_bonded_vs_oracle(lib, orc):
     imp = t.dihedrals[::7]
     ip = np.stack([np.full(len(imp), 0.01), np.linspace(-2.0, 2.0, len(imp))], 1)
     s.set_impropers(imp, ip)
-    s.compute_forces(lib.MASK_ALL)
+    s.compute_forces(lib.mask(lib.TERM_BOND, lib.TERM_ANGLE, lib.TERM_DIHEDRAL, lib.TERM_IMPROPER))
     f = s.get_forces()
     e, _ = s.get_energies()
     fb, eb = orc.bonds(c.positions, c.box, t.bonds, kb)

@@ -105,19 +105,34 @@ def test_pair_set_4_cells_superset_of_reference(lib, golden, orc):
         assert np.any(d > 1)
 
 
-def test_lj_forces_four_cell_box_match_reference(lib, golden):
-    """Where the reference's pair set is incomplete its forces differ from
-    the GPU's by exactly the dropped pairs' contribution; with the oracle
-    evaluated on the reference pair set the GPU matches the reference."""
-    pos = golden["sp50_positions"].astype(np.float64)
+def test_lj_forces_four_cell_box_match_reference(lib, golden, orc):
+    """Where the reference's pair set is incomplete (4^3 cells) its forces
+    differ from the GPU's by exactly the contribution of the pairs it drops."""
+    pos32 = golden["sp50_positions"]
+    pos = pos32.astype(np.float64)
     n = pos.shape[0]
-    s = make_system(lib, n, 50.0, lj=golden["sp50_lj_params"].astype(np.float64),
-                    charges=np.zeros(n), bonded=np.full((n, 1), -1), cutoff=12.0, positions=pos)
+    p = golden["sp50_lj_params"].astype(np.float64)
+    s = make_system(lib, n, 50.0, lj=p, charges=np.zeros(n), bonded=np.full((n, 1), -1),
+                    cutoff=12.0, positions=pos)
     s.compute_forces(lib.mask(lib.TERM_LJ))
     f = s.get_forces()
     ref = golden["sp50_forces"].astype(np.float64)
-    # the dropped pairs are few and long range (r close to rc): tiny force share
-    assert rel_rms(f, ref) < 1e-2
+    refset = pairs_to_set(orc.ref_pairs(pos32, np.full(3, 50.0, np.float32), 12.0,
+                                        golden["sp50_cell_index"], golden["sp50_num_cell_vec"],
+                                        np.full((n, 1), -1)))
+    dropped = np.array(sorted(pairs_to_set(orc.pairs_bruteforce(pos, 50.0, 12.0)) - refset))
+    d = pos[dropped[:, 1]] - pos[dropped[:, 0]]
+    d -= 50.0 * np.round(d / 50.0)
+    r2 = (d ** 2).sum(1)
+    eps = np.sqrt(p[dropped[:, 0], 0] * p[dropped[:, 1], 0])
+    sig = 0.5 * (p[dropped[:, 0], 1] + p[dropped[:, 1], 1])
+    s6 = (sig ** 2 / r2) ** 3
+    fr = 24 * eps * (2 * s6 * s6 - s6) / r2
+    f_drop = np.zeros((n, 3))
+    np.add.at(f_drop, dropped[:, 1], fr[:, None] * d)
+    np.add.at(f_drop, dropped[:, 0], -fr[:, None] * d)
+    assert rel_rms(f, ref + f_drop) <= 1e-5
+    assert rel_rms(f, ref) > 1e-3     # the defect is visible
 
 
 def test_bare_coulomb_four_atoms_matches_reference(lib, golden):
@@ -242,3 +257,22 @@ def test_cutoff_validation(lib):
     s = lib.System(10, 20.0)
     with pytest.raises(CellListPoorDefinedError):
         s.nonbonded_config(10.5)
+
+
+def test_overlapping_atoms_raise_fixed_point_overflow(lib):
+    """Two LJ atoms 0.2 A apart give forces ~1e13, outside the int64
+    fixed-point range (|F| < 2^31 internal units): the kernel's own check
+    reports it instead of returning a wrapped sum."""
+    from mdpy_gb300.error import FixedPointOverflowError
+
+    x = np.array([[1.0, 1.0, 1.0], [1.2, 1.0, 1.0]])
+    s = make_system(lib, 2, 30.0, charges=np.zeros(2),
+                    lj=np.tile([6.4e-5, 3.15, 6.4e-5, 3.15], (2, 1)), bonded=np.full((2, 1), -1),
+                    cutoff=12.0, positions=x)
+    s.compute_forces(lib.mask(lib.TERM_LJ))
+    with pytest.raises(FixedPointOverflowError):
+        s.get_forces()
+    # the status is cleared once reported; a sane configuration works again
+    s.set_positions(np.array([[1.0, 1.0, 1.0], [4.5, 1.0, 1.0]]))
+    s.compute_forces(lib.mask(lib.TERM_LJ))
+    assert np.all(np.isfinite(s.get_forces()))
