@@ -221,8 +221,6 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
     mdg_system *s = new mdg_system();
     s->device = device;
     s->n = n_atoms;
-    s->n_pad = (n_atoms + kCluster - 1) / kCluster * kCluster;
-    s->n_clusters = s->n_pad / kCluster;
     for (int d = 0; d < 3; ++d) s->box[d] = box[d];
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -230,7 +228,7 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
         return cuda_fail(e, "cudaStreamCreate");
     }
     s->stream = s->own_stream;
-    const int n = s->n, np = s->n_pad;
+    const int n = s->n;
 #define AL(ptr, cnt)                     \
     if ((rc = dalloc(&(ptr), (cnt)))) { \
         mdg_system_destroy(s);          \
@@ -240,18 +238,11 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
     AL(s->inv_mass, n);
     AL(s->charge, n);
     AL(s->lj, n);
-    AL(s->perm, np);
     AL(s->inv_perm, n);
-    AL(s->q_sorted, np);
-    AL(s->prm_sorted, np);
-    AL(s->cluster_partner_range, s->n_clusters);
     AL(s->atom_key, n);
     AL(s->tmp_perm, n);
     AL(s->x, 3 * (size_t)n);
     AL(s->v, 3 * (size_t)n);
-    AL(s->f, 3 * (size_t)np);
-    AL(s->xq, np);
-    AL(s->bbox, 2 * (size_t)s->n_clusters);
     AL(s->energy, kEnergySlots);
     AL(s->status, 1);
     AL(s->stats, 4);
@@ -259,13 +250,11 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
     AL(s->fout, 3 * (size_t)n);
     AL(s->dump_count, 1);
     AL(s->partners, 1);
-    AL(s->partners_sorted, 1);
 #undef AL
     cudaMemset(s->energy, 0, sizeof(long long) * kEnergySlots);
     cudaMemset(s->status, 0, sizeof(int));
     cudaMemset(s->step_dev, 0, sizeof(unsigned long long));
     cudaMemset(s->v, 0, sizeof(double) * 3 * n);
-    cudaMemset(s->f, 0, sizeof(unsigned long long) * 3 * np);
     cudaMemset(s->lj, 0, sizeof(float4) * n);
     cudaMemset(s->charge, 0, sizeof(float) * n);
     // masses default to 1 (inv 1) so kinetic terms are defined before set_masses
@@ -313,6 +302,8 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->atom_key);
     dfree(s->tmp_perm);
     dfree(s->scan_blocks);
+    dfree(s->col_ncl);
+    dfree(s->col_cl_start);
     dfree(s->x);
     dfree(s->v);
     dfree(s->f);

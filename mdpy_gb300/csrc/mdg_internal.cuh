@@ -1,6 +1,8 @@
 // mdg_internal.cuh -- shared definitions of libmdg's translation units.
 //
-// Data layout in HBM (per system; n atoms, n_pad = 32 * ceil(n/32)):
+// Data layout in HBM (per system; n atoms, cluster order holds n_pad slots =
+// 32 * (ceil(n/32) + number of sort columns): every column is padded to whole
+// clusters, so padding slots sit between columns):
 //   x, v            double[n][3]        atom order (FP64 state, as mdpy's State)
 //   f               int64 [3][n_pad]    cluster (sorted) order, fixed point 2^-32,
 //                                       SoA so a cluster's 32 atoms are one
@@ -102,9 +104,12 @@ struct mdg_system {
     int *partners_sorted = nullptr;
     int2 *cluster_partner_range = nullptr;
 
-    // spatial sort scratch
+    // spatial sort scratch: ncell = (columns x, columns y, height bins);
+    // n_cells = number of (column, height bin) keys
     int ncell[3] = {0, 0, 0};
     int n_cells = 0;
+    int n_cols = 0;
+    int *col_ncl = nullptr, *col_cl_start = nullptr;
     int *cell_rank = nullptr, *cell_count = nullptr, *cell_start = nullptr,
         *cell_cursor = nullptr, *atom_key = nullptr, *tmp_perm = nullptr, *scan_blocks = nullptr;
     int n_scan_blocks = 0;
@@ -178,7 +183,7 @@ cudaError_t launch_kinetic(mdg_system *s);
 cudaError_t launch_forces_out(mdg_system *s);
 cudaError_t launch_positions_out(mdg_system *s, double *out);
 cudaError_t launch_noise(mdg_system *s, uint64_t step, float *out);
-int prepare_sort_grid(mdg_system *s);   // host: choose fine cells, upload Morton ranks
+int prepare_sort_grid(mdg_system *s);   // host: column grid + cluster-order buffers
 int pme_setup(mdg_system *s);           // host: grids, plans, influence function
 void pme_free(mdg_system *s);
 }  // namespace mdg

@@ -10,15 +10,18 @@
 // and adds the Ewald real-space term k q_i q_j erfc(beta r)/r (MDG_COUL_EWALD),
 // which mdpy v0.2.1 does not have, plus an optional CHARMM switch for LJ.
 //
-// Design (GB300): one CTA of 4 warps per 32-atom i-cluster I.
-//   1. warp 0 walks the cluster bounding boxes J >= I (half shell) and keeps,
-//      in shared memory, every (J, periodic image) whose box lies within rc
-//      of I's box -- candidate compaction with __ballot_sync;
-//   2. the 4 warps take candidates round-robin; for each, every lane tests one
-//      j atom against I's bounding box, and the survivors are appended (warp
-//      ballot + popc, no atomics) to a 64-entry per-warp ring buffer in
-//      shared memory, already shifted to the right periodic image and with a
-//      32-bit exclusion mask (which i lanes must skip this j);
+// Design (GB300): kSplit = 4 independent single-warp CTAs per 32-atom
+// i-cluster I (no block barrier: a warp that finishes early frees its slot).
+//   1. each warp walks its own interleaved batches of cluster bounding boxes
+//      (a balanced half shell: the cluster pair {I, J} belongs to one of the
+//      two by the parity of I + J) and takes every (J, periodic image) whose
+//      box lies within rc of I's box -- __ballot_sync over 32 clusters at a
+//      time, no candidate list and no block barrier;
+//   2. for each candidate every lane tests one j atom against I's bounding
+//      box, and the survivors are appended (warp ballot + popc, no atomics)
+//      to a 64-entry per-warp ring buffer in shared memory, already shifted
+//      to the right periodic image and with a 32-bit exclusion mask (which i
+//      lanes must skip this j);
 //   3. each full chunk of 32 j entries is swept against the warp's 32 i atoms
 //      in 32 rotation steps: at step t lane l pairs its i atom with entry
 //      (l+t) mod 32, keeps the i force in registers and passes the j force
@@ -35,8 +38,7 @@
 namespace mdg {
 namespace {
 
-constexpr int kWarps = 4;
-constexpr int kCandCap = 2048;
+constexpr int kSplit = 4;  // work items (one warp each) per i-cluster
 constexpr int kRing = 64;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -78,23 +80,29 @@ __device__ __forceinline__ void decode_shift(int code, const NbArgs &a, float &s
     sz = (float)(code % 3 - 1) * a.L[2];
 }
 
-template <int COUL, bool SWITCH, bool ENERGY, bool DUMP>
-__global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
-    __shared__ int s_cand[kCandCap];
-    __shared__ int s_ncand, s_next;
-    __shared__ float4 s_jx[kWarps][kRing];
-    __shared__ float2 s_jp[kWarps][kRing];
-    __shared__ int2 s_jm[kWarps][kRing];
-    __shared__ float s_fi[3][kWarps][32];
-    __shared__ double s_e[2][kWarps];
+// one j entry staged in shared memory: shifted coordinates + charge, LJ
+// parameters, cluster-order index, exclusion mask of the 32 i lanes
+struct JEntry {
+    float4 xq;
+    float2 prm;
+    int jk;
+    unsigned mask;
+};
 
-    const int I = blockIdx.x;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+template <int COUL, bool SWITCH, bool ENERGY, bool DUMP>
+__global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
+    __shared__ JEntry s_j[kRing];
+
+    const int I = blockIdx.x / kSplit;     // i-cluster
+    const int part = blockIdx.x % kSplit;  // which quarter of the candidate scan
+    const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
+    if (cI.w == 0.f) return;  // all-padding cluster
+    const int lane = threadIdx.x;
     const unsigned lt = (1u << lane) - 1u;
     const int ik = I * kCluster + lane;
     const float4 xi = a.xq[ik];
     const float2 pi = a.prm[ik];
-    const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
+    const bool i_real = xi.x < 0.5f * kFarAway;
     const int2 rI = a.prange[I];
     const int ilo = I * kCluster;
 
@@ -103,23 +111,23 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
     unsigned long long n_eval = 0, n_in = 0;
     int jbase = 0, jcount = 0;
 
-    // sweep of one 32-entry chunk starting at ring slot `base`
+    // sweep of one 32-entry chunk starting at ring slot `base` (0 or 32)
     auto chunk = [&](int base) {
         float fjx = 0.f, fjy = 0.f, fjz = 0.f;
         float c_lj = 0.f, c_c = 0.f;
 #pragma unroll 4
         for (int t = 0; t < 32; ++t) {
-            const int e = (base + ((lane + t) & 31)) & (kRing - 1);
-            const float4 xj = s_jx[warp][e];
-            const float2 pj = s_jp[warp][e];
-            const unsigned mk = (unsigned)s_jm[warp][e].y;
+            const JEntry &je = s_j[base + ((lane + t) & 31)];
+            const float4 xj = je.xq;
+            const float2 pj = je.prm;
+            const unsigned mk = je.mask;
             const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const bool inc = (r2 <= a.rc2) && !((mk >> lane) & 1u);
             if (DUMP && inc) {
                 unsigned long long slot = atomicAdd(a.dump_count, 1ull);
                 if ((long long)slot < a.dump_cap) {
-                    int pj_atom = a.perm[s_jm[warp][e].x], pi_atom = a.perm[ik];
+                    int pj_atom = a.perm[je.jk], pi_atom = a.perm[ik];
                     a.dump[2 * slot] = min(pi_atom, pj_atom);
                     a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
                 }
@@ -133,16 +141,19 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
                 const float s2 = sig * sig * rinv2;
                 const float s6 = s2 * s2 * s2;
                 const float c6 = pi.y * pj.y * s6;
-                elj = c6 * (s6 - 1.0f);
                 float flj = c6 * fmaf(12.0f, s6, -6.0f) * rinv2;
                 if (SWITCH) {
-                    if (r2s > a.rs2) {
-                        const float u = a.rc2 - r2s;
-                        const float sw = u * u * fmaf(2.0f, r2s, a.rc2 - 3.0f * a.rs2) * a.sw_inv_den;
-                        const float dsw = 12.0f * u * (a.rs2 - r2s) * a.sw_inv_den;
-                        flj = flj * sw - elj * dsw;
-                        elj *= sw;
-                    }
+                    // CHARMM switch, branch free: below rs the clamped r^2 gives
+                    // sw = 1 and dsw = 0 exactly
+                    elj = c6 * (s6 - 1.0f);
+                    const float r2c = fmaxf(r2s, a.rs2);
+                    const float u = a.rc2 - r2c;
+                    const float sw = u * u * fmaf(2.0f, r2c, a.rc2 - 3.0f * a.rs2) * a.sw_inv_den;
+                    const float dsw = 12.0f * u * (a.rs2 - r2c) * a.sw_inv_den;
+                    flj = fmaf(flj, sw, -elj * dsw);
+                    elj *= sw;
+                } else if (ENERGY) {
+                    elj = c6 * (s6 - 1.0f);
                 }
                 fr = flj;
             }
@@ -178,8 +189,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
             fjy = __shfl_sync(kFull, fjy, src);
             fjz = __shfl_sync(kFull, fjz, src);
         }
-        const int e = (base + lane) & (kRing - 1);
-        const int jk = s_jm[warp][e].x;
+        const int jk = s_j[base + lane].jk;
         if (jk >= 0 && !DUMP) {
             if (!(fabsf(fjx) < kFixLimit && fabsf(fjy) < kFixLimit && fabsf(fjz) < kFixLimit))
                 raise_status(a.status, MDG_ERR_OVERFLOW);
@@ -195,175 +205,154 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
         __syncwarp();
     };
 
-    int Jstart = I;
-    for (;;) {
-        // ---- 1. cluster candidates (warp 0) -----------------------------
-        if (warp == 0) {
-            int nc = 0;
-            int J0 = Jstart;
-            for (; J0 < a.n_clusters; J0 += 32) {
-                const int J = J0 + lane;
-                const bool valid = J < a.n_clusters;
-                float4 cJ = make_float4(0.f, 0.f, 0.f, 0.f), hJ = cJ;
-                if (valid) {
-                    cJ = a.bbox[2 * J];
-                    hJ = a.bbox[2 * J + 1];
-                }
-                const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
-                const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
-                int ncode = 0;
-                float g2 = 0.f;
-                bool multi = false;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    float nk = -rintf(d[k] * a.invL[k]);
-                    nk = fminf(fmaxf(nk, -1.f), 1.f);
-                    const float dd = fmaf(nk, a.L[k], d[k]);
-                    const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
-                    g2 = fmaf(gap, gap, g2);
-                    ncode = ncode * 3 + (int)nk + 1;
-                    multi = multi || (h[k] + a.rc >= 0.5f * a.L[k]);
-                }
-                multi = multi && valid;
-                const bool near_hit = valid && g2 <= a.rc2;
-                const bool any_multi = __any_sync(kFull, multi);
-                if (nc + (any_multi ? 32 * 27 : 32) > kCandCap) break;  // next round
-                if (any_multi) {
-                    for (int code = 0; code < 27; ++code) {
-                        bool hit;
-                        if (multi) {
-                            const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
-                            float gg = 0.f;
-#pragma unroll
-                            for (int k = 0; k < 3; ++k) {
-                                const float dd = fmaf((float)s3[k], a.L[k], d[k]);
-                                const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
-                                gg = fmaf(gap, gap, gg);
-                            }
-                            hit = gg <= a.rc2;
-                        } else {
-                            hit = near_hit && code == ncode;
-                        }
-                        const unsigned b = __ballot_sync(kFull, hit);
-                        if (hit) s_cand[nc + __popc(b & lt)] = (J << 5) | code;
-                        nc += __popc(b);
-                    }
-                } else {
-                    const unsigned b = __ballot_sync(kFull, near_hit);
-                    if (near_hit) s_cand[nc + __popc(b & lt)] = (J << 5) | ncode;
-                    nc += __popc(b);
-                }
-            }
-            if (lane == 0) {
-                s_ncand = nc;
-                s_next = J0;
-            }
-        }
-        __syncthreads();
-        const int ncand = s_ncand, next = s_next;
-
-        // ---- 2./3. atom compaction and chunk sweeps ---------------------
-        for (int c = warp; c < ncand; c += kWarps) {
-            const int cc = s_cand[c];
-            const int J = cc >> 5;
-            float sx, sy, sz;
-            decode_shift(cc & 31, a, sx, sy, sz);
-            const int jk = J * kCluster + lane;
-            float4 xj = a.xq[jk];
-            xj.x += sx;
-            xj.y += sy;
-            xj.z += sz;
-            const float gx = fmaxf(fabsf(xj.x - cI.x) - hI.x, 0.f);
-            const float gy = fmaxf(fabsf(xj.y - cI.y) - hI.y, 0.f);
-            const float gz = fmaxf(fabsf(xj.z - cI.z) - hI.z, 0.f);
-            const bool hit = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) <= a.rc2;
-            const unsigned b = __ballot_sync(kFull, hit);
-            if (b == 0u) continue;
+    // one candidate (J, image) found by the scan: test J's atoms against I's box
+    // and append the survivors to this warp's ring (chunk sweeps when full)
+    auto candidate = [&](int J, int code) {
+        float sx, sy, sz;
+        decode_shift(code, a, sx, sy, sz);
+        const int jk = J * kCluster + lane;
+        float4 xj = a.xq[jk];
+        xj.x += sx;
+        xj.y += sy;
+        xj.z += sz;
+        const float gx = fmaxf(fabsf(xj.x - cI.x) - hI.x, 0.f);
+        const float gy = fmaxf(fabsf(xj.y - cI.y) - hI.y, 0.f);
+        const float gz = fmaxf(fabsf(xj.z - cI.z) - hI.z, 0.f);
+        const bool hit = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) <= a.rc2;
+        const unsigned b = __ballot_sync(kFull, hit);
+        if (b == 0u) return;
+        if (hit) {
             unsigned m = 0u;
-            if (hit) {
-                if (J == I) m = kFull << lane;  // half shell inside the cluster
-                if (rI.y >= J * kCluster && rI.x < (J + 1) * kCluster) {
-                    for (int w = 0; w < a.pw; ++w) {
-                        const int p = a.partners[(size_t)jk * a.pw + w];
-                        if (p >= 0) {
-                            const int pk = (p & 0x3fffffff) - ilo;
-                            if (pk >= 0 && pk < kCluster) m |= 1u << pk;
-                        }
+            if (J == I) m = kFull << lane;  // half shell inside the cluster
+            if (rI.y >= J * kCluster && rI.x < (J + 1) * kCluster) {
+                for (int w = 0; w < a.pw; ++w) {
+                    const int p = a.partners[(size_t)jk * a.pw + w];
+                    if (p >= 0) {
+                        const int pk = (p & 0x3fffffff) - ilo;
+                        if (pk >= 0 && pk < kCluster) m |= 1u << pk;
                     }
                 }
-                const int pos = (jbase + jcount + __popc(b & lt)) & (kRing - 1);
-                s_jx[warp][pos] = xj;
-                s_jp[warp][pos] = a.prm[jk];
-                s_jm[warp][pos] = make_int2(jk, (int)m);
             }
-            jcount += __popc(b);
-            __syncwarp();
-            if (jcount >= 32) {
-                chunk(jbase);
-                jbase = (jbase + 32) & (kRing - 1);
-                jcount -= 32;
+            const int pos = (jbase + jcount + __popc(b & lt)) & (kRing - 1);
+            JEntry e;
+            e.xq = xj;
+            e.prm = a.prm[jk];
+            e.jk = jk;
+            e.mask = m;
+            s_j[pos] = e;
+        }
+        jcount += __popc(b);
+        __syncwarp();
+        if (jcount >= 32) {
+            chunk(jbase);
+            jbase = (jbase + 32) & (kRing - 1);
+            jcount -= 32;
+        }
+    };
+
+    // Candidate clusters.  Work item `part` scans batches part, part + kSplit,
+    // ... of 32 clusters, so the kSplit warps of one i-cluster share its
+    // neighbourhood without talking to each other.
+    // Balanced half shell: the cluster pair {I, J} (I != J) belongs to I when
+    // I < J and I + J is odd, or when I > J and I + J is even -- every cluster
+    // owns about half of its neighbours whatever its index; J == I is kept and
+    // split by the lane mask.  Periodic images: the nearest image of J's box
+    // centre, or all 27 when a box pair spans half the box.
+    unsigned n_cand = 0;
+    for (int J0 = part * 32; J0 < a.n_clusters; J0 += kSplit * 32) {
+        const int J = J0 + lane;
+        bool valid = J < a.n_clusters;
+        if (valid && J != I) valid = ((I + J) & 1) == (I < J ? 1 : 0);
+        float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+               hJ = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) {
+            cJ = a.bbox[2 * J];
+            hJ = a.bbox[2 * J + 1];
+        }
+        const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+        const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+        int ncode = 0;
+        float g2 = 0.f;
+        bool multi = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float nk = -rintf(d[k] * a.invL[k]);
+            nk = fminf(fmaxf(nk, -1.f), 1.f);
+            const float dd = fmaf(nk, a.L[k], d[k]);
+            const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+            g2 = fmaf(gap, gap, g2);
+            ncode = ncode * 3 + (int)nk + 1;
+            multi = multi || (h[k] + a.rc >= 0.5f * a.L[k]);
+        }
+        valid = valid && cJ.w > 0.f;
+        multi = multi && valid;
+        const bool near_hit = valid && g2 <= a.rc2;
+        const bool any_multi = __any_sync(kFull, multi);
+        const int passes = any_multi ? 27 : 1;
+        for (int pass = 0; pass < passes; ++pass) {
+            bool hit;
+            int code;
+            if (any_multi) {
+                code = pass;
+                if (multi) {
+                    const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
+                    float gg = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const float dd = fmaf((float)s3[k], a.L[k], d[k]);
+                        const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                        gg = fmaf(gap, gap, gg);
+                    }
+                    hit = gg <= a.rc2;
+                } else {
+                    hit = near_hit && code == ncode;
+                }
+            } else {
+                code = ncode;
+                hit = near_hit;
+            }
+            unsigned b = __ballot_sync(kFull, hit);
+            if (ENERGY) n_cand += __popc(b);
+            while (b) {
+                const int src = __ffs(b) - 1;
+                b &= b - 1;
+                candidate(__shfl_sync(kFull, J, src), __shfl_sync(kFull, code, src));
             }
         }
-        __syncthreads();
-        if (next >= a.n_clusters) break;
-        Jstart = next;
     }
     if (jcount > 0) {
         const int pos = (jbase + lane) & (kRing - 1);
         if (lane >= jcount) {
-            s_jx[warp][pos] = make_float4(kFarAway, kFarAway, kFarAway, 0.f);
-            s_jp[warp][pos] = make_float2(0.f, 0.f);
-            s_jm[warp][pos] = make_int2(-1, (int)kFull);
+            JEntry e;
+            e.xq = make_float4(kFarAway, kFarAway, kFarAway, 0.f);
+            e.prm = make_float2(0.f, 0.f);
+            e.jk = -1;
+            e.mask = kFull;
+            s_j[pos] = e;
         }
         __syncwarp();
         chunk(jbase);
     }
 
-    // ---- i forces and energies ------------------------------------------
-    s_fi[0][warp][lane] = fix;
-    s_fi[1][warp][lane] = fiy;
-    s_fi[2][warp][lane] = fiz;
+    // ---- this work item's share of the i forces and energies -------------
+    if (!DUMP && i_real) {
+        if (!(fabsf(fix) < kFixLimit && fabsf(fiy) < kFixLimit && fabsf(fiz) < kFixLimit))
+            raise_status(a.status, MDG_ERR_OVERFLOW);
+        fix_red(&a.f[ik], to_fix(fix));
+        fix_red(&a.f[a.n_pad + ik], to_fix(fiy));
+        fix_red(&a.f[2 * a.n_pad + ik], to_fix(fiz));
+    }
     if (ENERGY) {
         const double el = warp_sum_d(acc_lj), ee = warp_sum_d(acc_c);
         if (lane == 0) {
-            s_e[0][warp] = el;
-            s_e[1][warp] = ee;
-        }
-    }
-    __syncthreads();
-    if (warp == 0 && !DUMP) {
-        float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            sx += s_fi[0][w][lane];
-            sy += s_fi[1][w][lane];
-            sz += s_fi[2][w][lane];
-        }
-        if (ik < a.n) {
-            if (!(fabsf(sx) < kFixLimit && fabsf(sy) < kFixLimit && fabsf(sz) < kFixLimit))
-                raise_status(a.status, MDG_ERR_OVERFLOW);
-            fix_red(&a.f[ik], to_fix(sx));
-            fix_red(&a.f[a.n_pad + ik], to_fix(sy));
-            fix_red(&a.f[2 * a.n_pad + ik], to_fix(sz));
-        }
-        if (ENERGY && lane == 0) {
-            double el = 0.0, ee = 0.0;
-            for (int w = 0; w < kWarps; ++w) {
-                el += s_e[0][w];
-                ee += s_e[1][w];
-            }
             if (!(fabs(el) < kFixLimit && fabs(ee) < kFixLimit))
                 raise_status(a.status, MDG_ERR_OVERFLOW);
             fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix_d(el));
             fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix_d(ee));
-        }
-    }
-    if (ENERGY && lane == 0) {
-        atomicAdd(&a.stats[0], n_eval);
-        atomicAdd(&a.stats[1], n_in);
-        if (warp == 0) {
-            atomicAdd(&a.stats[2], (unsigned long long)s_ncand);
-            atomicAdd(&a.stats[3], 1ull);
+            atomicAdd(&a.stats[0], n_eval);
+            atomicAdd(&a.stats[1], n_in);
+            atomicAdd(&a.stats[2], (unsigned long long)n_cand);
+            if (part == 0) atomicAdd(&a.stats[3], 1ull);
         }
     }
 }
@@ -373,19 +362,21 @@ __global__ void __launch_bounds__(kWarps * 32) k_nonbonded(NbArgs a) {
 // i atom, j atoms staged through shared memory in tiles, forces on i only.
 __global__ void __launch_bounds__(256) k_coulomb_bare(NbArgs a) {
     __shared__ float4 s_x[256];
+    // sorted slots, padding included; uncharged slots (padding has q = 0)
+    // contribute nothing and are skipped
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool iv = i < a.n;
-    const float4 xi = iv ? a.xq[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 xi = i < a.n_pad ? a.xq[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool iv = i < a.n_pad && xi.w != 0.f;
     float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-    for (int base = 0; base < a.n; base += 256) {
+    for (int base = 0; base < a.n_pad; base += 256) {
         const int jl = base + threadIdx.x;
-        s_x[threadIdx.x] = jl < a.n ? a.xq[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+        s_x[threadIdx.x] = jl < a.n_pad ? a.xq[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
         __syncthreads();
-        const int lim = min(256, a.n - base);
+        const int lim = min(256, a.n_pad - base);
         if (iv) {
             for (int t = 0; t < lim; ++t) {
                 const int j = base + t;
-                if (j == i) continue;
+                if (j == i || s_x[t].w == 0.f) continue;
                 bool excl = false;
                 for (int w = 0; w < a.pw; ++w) {
                     const int p = a.partners[(size_t)i * a.pw + w];
@@ -584,7 +575,7 @@ NbArgs make_args(mdg_system *s) {
 
 template <int COUL, bool SW>
 cudaError_t dispatch_nb(mdg_system *s, const NbArgs &a, int energy, int dump) {
-    dim3 grid(s->n_clusters), block(kWarps * 32);
+    dim3 grid(s->n_clusters * kSplit), block(32);
     if (dump)
         k_nonbonded<COUL, SW, false, true><<<grid, block, 0, s->stream>>>(a);
     else if (energy)
@@ -616,7 +607,7 @@ cudaError_t launch_nonbonded(mdg_system *s, unsigned mask, int energy, int dump)
         if (err != cudaSuccess) return err;
     }
     if (want_c && s->coul_mode == MDG_COUL_BARE && !dump) {
-        k_coulomb_bare<<<(s->n + 255) / 256, 256, 0, s->stream>>>(a);
+        k_coulomb_bare<<<(s->n_pad + 255) / 256, 256, 0, s->stream>>>(a);
         s->launches += 1;
         err = cudaGetLastError();
     }

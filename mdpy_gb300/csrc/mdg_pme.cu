@@ -85,9 +85,9 @@ __device__ __forceinline__ void frac(float x, float kl, int K, int &g0, float &w
 template <int P>
 __global__ void __launch_bounds__(256) k_spread(PmeArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n) return;
+    if (k >= a.n_pad) return;
     const float4 p = a.xq[k];
-    if (p.w == 0.f) return;
+    if (p.w == 0.f) return;  // padding slot or uncharged atom
     float tx[P], ty[P], tz[P], d[P];
     int gx, gy, gz;
     float w;
@@ -154,9 +154,9 @@ __global__ void __launch_bounds__(256) k_convolve(float2 *__restrict__ gc,
 template <int P>
 __global__ void __launch_bounds__(256) k_gather(PmeArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n) return;
+    if (k >= a.n_pad) return;
     const float4 p = a.xq[k];
-    if (p.w == 0.f) return;
+    if (p.w == 0.f) return;  // padding slot or uncharged atom
     float tx[P], ty[P], tz[P], dx[P], dy[P], dz[P];
     int gx, gy, gz;
     float w;
@@ -304,7 +304,7 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
     a.grid_i = (unsigned long long *)p.grid_i;
     a.phi = p.grid_r;
     a.f = s->f;
-    const int tb = 256, nb = (s->n + tb - 1) / tb;
+    const int tb = 256, nb = (s->n_pad + tb - 1) / tb;
     cudaStream_t st = s->stream;
     switch (p.order) {
         case 4: k_spread<4><<<nb, tb, 0, st>>>(a); break;

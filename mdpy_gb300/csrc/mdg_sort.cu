@@ -4,15 +4,21 @@
 // Replaces mdpy's CellList (mdpy/core/cell_list.py:83-116), which rebuilds a
 // dense padded (nx, ny, nz, max_per_cell) cell list from scratch on every
 // State.set_positions.  Here the atoms are re-sorted every `reorder_interval`
-// steps into Z-order (Morton) of fine cells so that each run of 32 sorted
-// atoms is a spatially compact cluster; between sorts only the cluster
-// bounding boxes are refreshed (k_pack).  Neighbour candidates are found on
-// the fly from those boxes in the pair kernel, so the sort interval affects
-// only efficiency, never which pairs are found.
+// steps into columns: the box is cut into an x-y grid of columns whose cross
+// section is the edge a = (32/rho)^(1/3) of a cube holding 32 atoms, atoms are
+// ordered by height inside each column, and every column is padded to a whole
+// number of 32-atom clusters.  A cluster is then a compact ~a x a x a block
+// (a ~ 7 A in water), which keeps the pair kernel's bounding-box candidates
+// tight.  Columns are visited in 2-D Z-order so that neighbouring clusters
+// have nearby indices.  Between sorts only the bounding boxes are refreshed
+// (k_pack); neighbour candidates are found from those boxes in the pair
+// kernel, so the sort interval affects efficiency only, never which pairs
+// are found.
 //
-// The sort is a deterministic counting sort: histogram of cell keys,
-// exclusive scan, scatter, then an insertion sort by atom index inside each
-// (small) cell, so a given configuration always yields the same order.
+// The sort is a deterministic counting sort over (column, height bin) keys:
+// histogram, exclusive scan, scatter, then an insertion sort by atom index
+// inside each (small) bin, so a given configuration always yields the same
+// order.  Padding slots carry perm = -1, charge 0 and a far-away position.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -26,12 +32,12 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanPerBlock = 2 * kScanThreads;
 
 __global__ void k_bin(double *__restrict__ x, int n, double bx, double by, double bz, int ncx,
-                      int ncy, int ncz, const int *__restrict__ cell_rank, int *__restrict__ key,
+                      int ncy, int nzb, const int *__restrict__ col_rank, int *__restrict__ key,
                       int *__restrict__ count, int *__restrict__ status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double L[3] = {bx, by, bz};
-    const int nc[3] = {ncx, ncy, ncz};
+    const int nc[3] = {ncx, ncy, nzb};
     int c[3];
     bool ok = true;
 #pragma unroll
@@ -46,7 +52,7 @@ __global__ void k_bin(double *__restrict__ x, int n, double bx, double by, doubl
         c[d] = k < 0 ? 0 : (k >= nc[d] ? nc[d] - 1 : k);
     }
     if (!ok) raise_status(status, MDG_ERR_PARTICLE_LOSS);
-    int k = cell_rank[(c[0] * ncy + c[1]) * ncz + c[2]];
+    int k = col_rank[c[0] * ncy + c[1]] * nzb + c[2];
     key[i] = k;
     atomicAdd(&count[k], 1);
 }
@@ -145,24 +151,48 @@ __global__ void k_cell_sort(const int *__restrict__ start, int ncells, int *__re
     }
 }
 
-__global__ void k_finish_perm(const int *__restrict__ tmp, int n, int n_pad, int *__restrict__ perm,
+// clusters per column (columns in rank order), then their exclusive scan
+__global__ void k_col_clusters(const int *__restrict__ start, int n_cols, int nzb,
+                               int *__restrict__ col_ncl) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cols) return;
+    const int cnt = start[(c + 1) * nzb] - start[c * nzb];
+    col_ncl[c] = (cnt + kCluster - 1) / kCluster;
+}
+
+__global__ void k_col_scan(const int *__restrict__ col_ncl, int n_cols,
+                           int *__restrict__ col_cl_start) {
+    int carry = 0;
+    for (int off = 0; off < n_cols; off += kScanPerBlock) {
+        int i = off + 2 * threadIdx.x;
+        int a = i < n_cols ? col_ncl[i] : 0, b = i + 1 < n_cols ? col_ncl[i + 1] : 0;
+        int ea, eb, tot;
+        block_scan2(a, b, ea, eb, tot);
+        if (i < n_cols) col_cl_start[i] = carry + ea;
+        if (i + 1 < n_cols) col_cl_start[i + 1] = carry + eb;
+        carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) col_cl_start[n_cols] = carry;
+}
+
+// atom of global rank g goes to its column's cluster block, in rank order
+__global__ void k_finish_perm(const int *__restrict__ tmp, const int *__restrict__ key, int n,
+                              int nzb, const int *__restrict__ start,
+                              const int *__restrict__ col_cl_start, int *__restrict__ perm,
                               int *__restrict__ inv_perm, const float *__restrict__ charge,
                               const float4 *__restrict__ lj, float *__restrict__ q_sorted,
                               float2 *__restrict__ prm_sorted) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_pad) return;
-    if (k < n) {
-        int i = tmp[k];
-        perm[k] = i;
-        inv_perm[i] = k;
-        q_sorted[k] = charge[i];
-        float4 p = lj[i];
-        prm_sorted[k] = make_float2(p.x, p.y);
-    } else {
-        perm[k] = -1;
-        q_sorted[k] = 0.0f;
-        prm_sorted[k] = make_float2(0.0f, 0.0f);
-    }
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int i = tmp[g];
+    const int cr = key[i] / nzb;
+    const int slot = kCluster * col_cl_start[cr] + (g - start[cr * nzb]);
+    perm[slot] = i;
+    inv_perm[i] = slot;
+    q_sorted[slot] = charge[i];
+    const float4 p = lj[i];
+    prm_sorted[slot] = make_float2(p.x, p.y);
 }
 
 // partners in sorted indices, bit 30 kept as the 1-4 flag: the pair kernel
@@ -238,61 +268,86 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ per
     }
     int cnt = __popc(__ballot_sync(0xffffffffu, valid));
     if (lane == 0) {
-        bbox[2 * warp] = make_float4(0.5f * (lox + hix), 0.5f * (loy + hiy), 0.5f * (loz + hiz),
-                                     (float)cnt);
-        bbox[2 * warp + 1] = make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy),
-                                         0.5f * (hiz - loz), 0.0f);
+        if (cnt == 0) {  // an all-padding cluster: far away, zero extent
+            bbox[2 * warp] = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+            bbox[2 * warp + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            bbox[2 * warp] = make_float4(0.5f * (lox + hix), 0.5f * (loy + hiy),
+                                         0.5f * (loz + hiz), (float)cnt);
+            bbox[2 * warp + 1] = make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy),
+                                             0.5f * (hiz - loz), 0.0f);
+        }
     }
 }
 
-inline unsigned spread_bits(unsigned v) {
-    v &= 0x3ff;
-    v = (v | (v << 16)) & 0x030000FF;
-    v = (v | (v << 8)) & 0x0300F00F;
-    v = (v | (v << 4)) & 0x030C30C3;
-    v = (v | (v << 2)) & 0x09249249;
+inline unsigned spread2(unsigned v) {
+    v &= 0xffff;
+    v = (v | (v << 8)) & 0x00FF00FF;
+    v = (v | (v << 4)) & 0x0F0F0F0F;
+    v = (v | (v << 2)) & 0x33333333;
+    v = (v | (v << 1)) & 0x55555555;
     return v;
+}
+
+template <typename T>
+int realloc_dev(T **p, size_t count) {
+    cudaFree(*p);
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, count * sizeof(T)) == cudaSuccess ? MDG_OK : MDG_ERR_NOMEM;
 }
 
 }  // namespace
 
-// host: fine-cell grid (~4 atoms per cell) and the Morton rank of each cell
+// host: column grid for this box and density, and every buffer whose size
+// depends on it (the cluster-order arrays are sized for the worst-case
+// padding: one partial cluster per column)
 int prepare_sort_grid(mdg_system *s) {
-    double V = s->box[0] * s->box[1] * s->box[2];
-    double rho = s->n / V;
-    double edge = std::cbrt(4.0 / std::max(rho, 1e-6));
-    int total = 1;
-    for (int d = 0; d < 3; ++d) {
-        int nc = (int)std::floor(s->box[d] / edge);
-        nc = std::max(1, std::min(nc, 1023));
-        s->ncell[d] = nc;
-        total *= nc;
-    }
-    std::vector<std::pair<unsigned, int>> codes(total);
-    for (int a = 0; a < s->ncell[0]; ++a)
-        for (int b = 0; b < s->ncell[1]; ++b)
-            for (int c = 0; c < s->ncell[2]; ++c) {
-                int lin = (a * s->ncell[1] + b) * s->ncell[2] + c;
-                unsigned code = spread_bits(a) | (spread_bits(b) << 1) | (spread_bits(c) << 2);
-                codes[lin] = {code, lin};
-            }
+    const double V = s->box[0] * s->box[1] * s->box[2];
+    const double rho = std::max(s->n / V, 1e-6);
+    const double a = std::cbrt((double)kCluster / rho);
+    const int ncx = std::max(1, std::min(4096, (int)std::lround(s->box[0] / a)));
+    const int ncy = std::max(1, std::min(4096, (int)std::lround(s->box[1] / a)));
+    const int nzb = std::max(1, std::min(8192, (int)std::lround(s->box[2] / (a / 8.0))));
+    const int n_cols = ncx * ncy;
+    const long long n_keys = (long long)n_cols * nzb;
+    if (n_keys > (1ll << 26)) return MDG_ERR_INVALID;
+    s->ncell[0] = ncx;
+    s->ncell[1] = ncy;
+    s->ncell[2] = nzb;
+    s->n_cols = n_cols;
+    s->n_cells = (int)n_keys;
+    std::vector<std::pair<unsigned, int>> codes(n_cols);
+    for (int cx = 0; cx < ncx; ++cx)
+        for (int cy = 0; cy < ncy; ++cy)
+            codes[cx * ncy + cy] = {spread2(cx) | (spread2(cy) << 1), cx * ncy + cy};
     std::sort(codes.begin(), codes.end());
-    std::vector<int> rank(total);
-    for (int r = 0; r < total; ++r) rank[codes[r].second] = r;
-    cudaFree(s->cell_rank);
-    cudaFree(s->cell_count);
-    cudaFree(s->cell_start);
-    cudaFree(s->cell_cursor);
-    cudaFree(s->scan_blocks);
-    s->n_cells = total;
-    s->n_scan_blocks = (total + kScanPerBlock - 1) / kScanPerBlock;
-    if (cudaMalloc(&s->cell_rank, sizeof(int) * total) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMalloc(&s->cell_count, sizeof(int) * total) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMalloc(&s->cell_start, sizeof(int) * (total + 1)) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMalloc(&s->cell_cursor, sizeof(int) * total) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMalloc(&s->scan_blocks, sizeof(int) * s->n_scan_blocks) != cudaSuccess)
-        return MDG_ERR_NOMEM;
-    if (cudaMemcpy(s->cell_rank, rank.data(), sizeof(int) * total, cudaMemcpyHostToDevice) !=
+    std::vector<int> rank(n_cols);
+    for (int r = 0; r < n_cols; ++r) rank[codes[r].second] = r;
+    s->n_scan_blocks = (int)((n_keys + kScanPerBlock - 1) / kScanPerBlock);
+    const int n_clusters = (s->n + kCluster - 1) / kCluster + n_cols;
+    const int n_pad = n_clusters * kCluster;
+    int rc = MDG_OK;
+    if ((rc = realloc_dev(&s->cell_rank, n_cols)) || (rc = realloc_dev(&s->cell_count, n_keys)) ||
+        (rc = realloc_dev(&s->cell_start, n_keys + 1)) ||
+        (rc = realloc_dev(&s->cell_cursor, n_keys)) ||
+        (rc = realloc_dev(&s->scan_blocks, s->n_scan_blocks)) ||
+        (rc = realloc_dev(&s->col_ncl, n_cols)) || (rc = realloc_dev(&s->col_cl_start, n_cols + 1)))
+        return rc;
+    if (n_pad != s->n_pad || !s->perm) {
+        s->n_pad = n_pad;
+        s->n_clusters = n_clusters;
+        if ((rc = realloc_dev(&s->perm, n_pad)) || (rc = realloc_dev(&s->q_sorted, n_pad)) ||
+            (rc = realloc_dev(&s->prm_sorted, n_pad)) || (rc = realloc_dev(&s->xq, n_pad)) ||
+            (rc = realloc_dev(&s->f, 3 * (size_t)n_pad)) ||
+            (rc = realloc_dev(&s->bbox, 2 * (size_t)n_clusters)) ||
+            (rc = realloc_dev(&s->cluster_partner_range, n_clusters)) ||
+            (rc = realloc_dev(&s->partners_sorted, (size_t)n_pad * std::max(s->pw, 1))))
+            return rc;
+        if (cudaMemset(s->f, 0, sizeof(unsigned long long) * 3 * n_pad) != cudaSuccess)
+            return MDG_ERR_CUDA;
+    }
+    if (cudaMemcpy(s->cell_rank, rank.data(), sizeof(int) * n_cols, cudaMemcpyHostToDevice) !=
         cudaSuccess)
         return MDG_ERR_CUDA;
     return MDG_OK;
@@ -304,6 +359,9 @@ cudaError_t launch_reorder(mdg_system *s) {
     const int tb = 256;
     cudaMemsetAsync(s->cell_count, 0, sizeof(int) * s->n_cells, st);
     cudaMemsetAsync(s->cell_cursor, 0, sizeof(int) * s->n_cells, st);
+    cudaMemsetAsync(s->perm, 0xff, sizeof(int) * s->n_pad, st);
+    cudaMemsetAsync(s->q_sorted, 0, sizeof(float) * s->n_pad, st);
+    cudaMemsetAsync(s->prm_sorted, 0, sizeof(float2) * s->n_pad, st);
     k_bin<<<(n + tb - 1) / tb, tb, 0, st>>>(s->x, n, s->box[0], s->box[1], s->box[2], s->ncell[0],
                                             s->ncell[1], s->ncell[2], s->cell_rank, s->atom_key,
                                             s->cell_count, s->status);
@@ -312,16 +370,20 @@ cudaError_t launch_reorder(mdg_system *s) {
     k_scan_top<<<1, kScanThreads, 0, st>>>(s->scan_blocks, s->n_scan_blocks);
     k_scan_final<<<s->n_scan_blocks, kScanThreads, 0, st>>>(s->cell_count, s->n_cells,
                                                             s->scan_blocks, s->cell_start);
+    k_col_clusters<<<(s->n_cols + tb - 1) / tb, tb, 0, st>>>(s->cell_start, s->n_cols,
+                                                             s->ncell[2], s->col_ncl);
+    k_col_scan<<<1, kScanThreads, 0, st>>>(s->col_ncl, s->n_cols, s->col_cl_start);
     k_scatter<<<(n + tb - 1) / tb, tb, 0, st>>>(s->atom_key, n, s->cell_start, s->cell_cursor,
                                                 s->tmp_perm);
     k_cell_sort<<<(s->n_cells + tb - 1) / tb, tb, 0, st>>>(s->cell_start, s->n_cells, s->tmp_perm);
-    k_finish_perm<<<(s->n_pad + tb - 1) / tb, tb, 0, st>>>(s->tmp_perm, n, s->n_pad, s->perm,
-                                                           s->inv_perm, s->charge, s->lj,
-                                                           s->q_sorted, s->prm_sorted);
+    k_finish_perm<<<(n + tb - 1) / tb, tb, 0, st>>>(s->tmp_perm, s->atom_key, n, s->ncell[2],
+                                                    s->cell_start, s->col_cl_start, s->perm,
+                                                    s->inv_perm, s->charge, s->lj, s->q_sorted,
+                                                    s->prm_sorted);
     k_partners_sorted<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, st>>>(
         s->perm, s->inv_perm, s->partners, s->pw, s->n_clusters, s->partners_sorted,
         s->cluster_partner_range);
-    s->launches += 8;
+    s->launches += 10;
     return cudaGetLastError();
 }
 

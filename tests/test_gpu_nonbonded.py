@@ -131,8 +131,14 @@ def test_lj_forces_four_cell_box_match_reference(lib, golden, orc):
     f_drop = np.zeros((n, 3))
     np.add.at(f_drop, dropped[:, 1], fr[:, None] * d)
     np.add.at(f_drop, dropped[:, 0], -fr[:, None] * d)
+    assert len(dropped) > 0
     assert rel_rms(f, ref + f_drop) <= 1e-5
-    assert rel_rms(f, ref) > 1e-3     # the defect is visible
+    # on the atoms of the dropped pairs, the pairs the reference misses account
+    # for the GPU-minus-reference difference (elsewhere both agree to float32)
+    hit = np.unique(dropped.reshape(-1))
+    before = np.sqrt(np.mean((f[hit] - ref[hit]) ** 2))
+    after = np.sqrt(np.mean((f[hit] - ref[hit] - f_drop[hit]) ** 2))
+    assert after < 0.3 * before
 
 
 def test_bare_coulomb_four_atoms_matches_reference(lib, golden):
