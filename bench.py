@@ -48,6 +48,10 @@ def parse():
     p.add_argument("--steps", type=int, default=3000)
     p.add_argument("--warmup", type=int, default=50)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="water90k", choices=["water90k", "batch256"],
+                   help="water90k: the 88k-atom box (default); batch256: 256 independent "
+                        "water boxes of 1.5k-12k atoms in one batch")
+    p.add_argument("--boxes", type=int, default=256)
     p.add_argument("--waters", type=int, default=30000)
     p.add_argument("--box", type=float, default=96.5)
     p.add_argument("--beads", type=int, default=500)
@@ -85,6 +89,140 @@ def make_ensemble(s, device):
     ens.state.set_positions(s.positions)
     ens.state.set_velocities(s.velocities)
     return ens, nb.ewald_beta
+
+
+BATCH_CUTOFF = 10.0
+
+
+def make_batch_members(n_boxes, seed):
+    """256 water boxes, atom counts log-uniform in [1500, 12000], each with a
+    PME grid of ~1 A spacing clipped to 24..48, cutoff 10 A."""
+    from mdpy_gb300 import batch, constraint as C, systems
+
+    ws = systems.water_box_batch(n_boxes, 1500, 12000, seed=seed)
+    members = []
+    for w in ws:
+        grid = min(48, max(24, systems.fft_friendly(int(round(w.box[0])))))
+        ens = batch.member(w.topology, w.pbc_matrix)
+        ens.add_constraints(
+            C.NonbondedConstraint(w.parameters["nonbonded"], BATCH_CUTOFF, ewald_error=EWALD_TOL),
+            C.PMEConstraint(grid_size=grid, ewald_error=EWALD_TOL, real_space_cutoff=BATCH_CUTOFF),
+            C.CharmmBondConstraint(w.parameters["bond"]),
+            C.CharmmAngleConstraint(w.parameters["angle"]))
+        ens.state.set_positions(w.positions)
+        ens.state.set_velocities(w.velocities)
+        members.append((w, ens, grid))
+    return members
+
+
+def time_steps(sysm, mask, steps, stream, flush):
+    import torch
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        sysm.integrate(1, mask, want_energy=False)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return sum(st.elapsed_time(en) for st, en in zip(starts, ends))
+
+
+def run_batch(a, world, rank, local):
+    """Batched form: every box in one device batch (one set of launches per
+    step, one CUDA graph per step), against the same boxes run one at a time
+    (a sample of every 8th box, scaled by its share of the atoms)."""
+    import torch
+
+    from mdpy_gb300 import _lib, batch, unit
+    from mdpy_gb300.ensemble import Ensemble
+    from mdpy_gb300.integrator import LangevinIntegrator
+
+    torch.cuda.set_device(local)
+    members = make_batch_members(a.boxes, seed=rank)
+    b = batch.EnsembleBatch([m[1] for m in members], device=local)
+    sysm = b.system
+    n = sysm.n
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sysm.set_stream(stream.cuda_stream)
+    integ = LangevinIntegrator(DT_FS, TEMPERATURE, FRICTION, seed=1000 + rank)
+    integ._configure(b)
+    mask = b.term_mask
+    sysm.set_graph_mode(_lib.GRAPH_STEP)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    sysm.integrate(max(a.warmup, 3), mask, want_energy=False)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = sysm.launch_count
+    ms_total = time_steps(sysm, mask, a.steps, stream, flush)
+    launches = sysm.launch_count - launches0
+    clk = clocks.stop()
+    ms_total = reduce_max(ms_total, world, device=torch.device("cuda", local)
+                          if world > 1 and os.environ.get("MDG_BENCH_BACKEND", "nccl") == "nccl"
+                          else None)
+    sysm.check_status()
+    ms_step = ms_total / a.steps
+    atom_steps = world * n * a.steps / (ms_total / 1000.0)
+    # per-box ns/day averaged over boxes = steps/s of the batch
+    ns_day_per_box = unit.ns_per_day(a.steps / (ms_total / 1000.0), DT_FS)
+    b.update()
+    pe = b.potential_energies
+
+    # the same boxes one at a time: every 8th box, each its own system
+    sample = members[::8]
+    single_ms, single_atoms = 0.0, 0
+    for w, _, grid in sample:
+        from mdpy_gb300 import constraint as C
+
+        ens = Ensemble(w.topology, w.pbc_matrix, device=local)
+        ens.add_constraints(
+            C.NonbondedConstraint(w.parameters["nonbonded"], BATCH_CUTOFF, ewald_error=EWALD_TOL),
+            C.PMEConstraint(grid_size=grid, ewald_error=EWALD_TOL, real_space_cutoff=BATCH_CUTOFF),
+            C.CharmmBondConstraint(w.parameters["bond"]),
+            C.CharmmAngleConstraint(w.parameters["angle"]))
+        ens.state.set_positions(w.positions)
+        ens.state.set_velocities(w.velocities)
+        ss = ens.system
+        ss.set_stream(stream.cuda_stream)
+        integ._configure(ens)
+        ss.set_graph_mode(_lib.GRAPH_STEP)
+        ss.integrate(5, mask, want_energy=False)
+        torch.cuda.synchronize()
+        reps = max(10, a.steps // 10)
+        single_ms += time_steps(ss, mask, reps, stream, flush) / reps
+        single_atoms += w.num_particles
+        ss.close()
+    one_at_a_time_ms = single_ms * (n / single_atoms)
+    if rank == 0:
+        sizes = [m[0].num_particles for m in members]
+        grids = sorted({m[2] for m in members})
+        line = {
+            "metric": "atom-steps/s, %d independent water boxes on 1 GB300" % a.boxes,
+            "value": atom_steps, "unit": "atom-steps/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch%d_water_1.5k-12k_atoms_rc%g_pme%d-%d_o4_langevin300K_1fs"
+                                   % (a.boxes, BATCH_CUTOFF, grids[0], grids[-1]),
+                       "atoms": n, "boxes": a.boxes, "atoms_min": min(sizes),
+                       "atoms_max": max(sizes), "pme_grids": grids,
+                       "l2": "flushed between timed steps (256 MB rewrite)", "form": "batched"},
+            "ns_per_day_per_box": ns_day_per_box,
+            "one_at_a_time": {"ms_per_step_all_boxes": one_at_a_time_ms,
+                              "atom_steps_per_s": n / (one_at_a_time_ms / 1000.0),
+                              "sample": "every 8th box (%d boxes, %d atoms) timed alone, scaled "
+                                        "by atoms" % (len(sample), single_atoms)},
+            "speedup_vs_one_at_a_time": one_at_a_time_ms / ms_step,
+            "finite_energies": bool(np.all(np.isfinite(pe))),
+            "gpu_launches": int(launches), "clocks": clk,
+        }
+        print(json.dumps(line))
+    return 0
 
 
 # --------------------------------------------------------------------------
@@ -293,6 +431,8 @@ def main():
     world, rank, local = dist_setup()
     if a.impl == "reference":
         return run_reference_arm(a, world, rank)
+    if a.workload == "batch256":
+        return run_batch(a, world, rank, local)
 
     import torch
 

@@ -87,8 +87,30 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
 MDG_API int mdg_system_destroy(mdg_system *sys);
 /* cudaStream_t passed as void*; NULL restores the system's own stream */
 MDG_API int mdg_system_set_stream(mdg_system *sys, void *stream);
-/* State.set_pbc_matrix (mdpy/core/state.py:47-54), diagonal only */
+/* State.set_pbc_matrix (mdpy/core/state.py:47-54), diagonal only; in a batch
+ * every system gets this box */
 MDG_API int mdg_system_set_box(mdg_system *sys, const double *box);
+
+/* ---- batches of independent systems (no reference counterpart: mdpy runs
+ * one Ensemble per process; a batch runs many small ensembles in one set of
+ * launches).  System q owns atoms [off_q, off_q + n_atoms[q]) of every per-atom
+ * array (off_q = sum of the earlier counts); it has its own box (boxes[3q..3q+2]),
+ * PME grid and energies; nonbonded, PME order/beta and integrator settings are
+ * shared.  Exclusion partners and bonded terms must stay inside one system.
+ * Forces, energies and trajectories of each system are those it would have
+ * alone, up to float rounding of the batched FFT.  A single system is a batch
+ * of one. */
+MDG_API int mdg_system_create_batch(int device, int n_systems, const int *n_atoms,
+                                    const double *boxes, mdg_system **out);
+MDG_API int mdg_num_systems(mdg_system *sys, int *n_systems);
+/* boxes (n_systems, 3) */
+MDG_API int mdg_system_set_boxes(mdg_system *sys, const double *boxes);
+/* PME with one grid per system: grids (n_systems, 3); systems with equal grids
+ * share one batched FFT */
+MDG_API int mdg_pme_config_batch(mdg_system *sys, const int *grids, int order, double beta);
+/* energies (n_systems, MDG_NUM_TERMS) and kinetic (n_systems) of the last
+ * evaluation, per system; either may be NULL */
+MDG_API int mdg_get_energies_batch(mdg_system *sys, double *energies, double *kinetic);
 
 /* ---- static parameters (bind_ensemble work) ----------------------------- */
 /* Topology.join masses/charges (mdpy/core/topology.py:59-70) */
@@ -140,7 +162,8 @@ MDG_API int mdg_compute_forces(mdg_system *sys, unsigned mask);
 /* Ensemble.forces / Constraint.forces: (n,3) FP64 in atom order */
 MDG_API int mdg_get_forces(mdg_system *sys, double *f, int where);
 /* energies[MDG_NUM_TERMS] of the last evaluation (reciprocal slot includes the
- * self, net-charge and exclusion terms) and the kinetic energy */
+ * self, net-charge and exclusion terms) and the kinetic energy; a batch
+ * reports the sums over its systems */
 MDG_API int mdg_get_energies(mdg_system *sys, double *energies, double *kinetic);
 /* Ensemble._update_kinetic_energy (mdpy/ensemble.py:63-71), FP64 */
 MDG_API int mdg_kinetic_energy(mdg_system *sys, double *kinetic);

@@ -45,6 +45,12 @@ _sys_p = ctypes.c_void_p
 SIGNATURES = {
     "mdg_version": [_c_int_p, _c_int_p],
     "mdg_system_create": [ctypes.c_int, ctypes.c_int, _c_dbl_p, ctypes.POINTER(_sys_p)],
+    "mdg_system_create_batch": [ctypes.c_int, ctypes.c_int, _c_int_p, _c_dbl_p,
+                                ctypes.POINTER(_sys_p)],
+    "mdg_num_systems": [_sys_p, _c_int_p],
+    "mdg_system_set_boxes": [_sys_p, _c_dbl_p],
+    "mdg_pme_config_batch": [_sys_p, _c_int_p, ctypes.c_int, ctypes.c_double],
+    "mdg_get_energies_batch": [_sys_p, _c_dbl_p, _c_dbl_p],
     "mdg_system_destroy": [_sys_p],
     "mdg_system_set_stream": [_sys_p, ctypes.c_void_p],
     "mdg_system_set_box": [_sys_p, _c_dbl_p],
@@ -130,16 +136,38 @@ def _dp(a):
 
 
 class System:
-    """One device-resident MD system (``mdg_system``)."""
+    """One device-resident MD system (``mdg_system``).
 
-    def __init__(self, n_atoms, box, device=0):
+    ``System.batch(n_atoms_list, boxes)`` makes a batch of independent
+    systems that share one set of launches: per-atom arrays are the systems'
+    arrays concatenated in order, and ``get_energies_batch`` reports each
+    system's energies."""
+
+    def __init__(self, n_atoms, box, device=0, _batch=None):
         self._lib = load()
-        self.n = int(n_atoms)
         self.device = int(device)
-        box = _f64(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
         h = _sys_p()
-        check(self._lib.mdg_system_create(self.device, self.n, _dp(box), ctypes.byref(h)))
+        if _batch is None:
+            self.n = int(n_atoms)
+            self.n_systems = 1
+            self.atoms_per_system = np.array([self.n], dtype=np.int64)
+            box = _f64(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+            check(self._lib.mdg_system_create(self.device, self.n, _dp(box), ctypes.byref(h)))
+        else:
+            counts = np.ascontiguousarray(_batch[0], dtype=np.int32).reshape(-1)
+            boxes = _f64(np.broadcast_to(np.asarray(_batch[1], dtype=np.float64),
+                                         (counts.size, 3)))
+            self.n = int(counts.sum())
+            self.n_systems = int(counts.size)
+            self.atoms_per_system = counts.astype(np.int64)
+            check(self._lib.mdg_system_create_batch(
+                self.device, self.n_systems, counts.ctypes.data_as(_c_int_p), _dp(boxes),
+                ctypes.byref(h)))
         self._h = h
+
+    @classmethod
+    def batch(cls, n_atoms, boxes, device=0):
+        return cls(None, None, device=device, _batch=(n_atoms, boxes))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -163,6 +191,10 @@ class System:
     def set_box(self, box):
         box = _f64(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
         check(self._lib.mdg_system_set_box(self._h, _dp(box)))
+
+    def set_boxes(self, boxes):
+        boxes = _f64(np.broadcast_to(np.asarray(boxes, dtype=np.float64), (self.n_systems, 3)))
+        check(self._lib.mdg_system_set_boxes(self._h, _dp(boxes)))
 
     def set_masses(self, m):
         m = _f64(m).reshape(-1)
@@ -255,6 +287,19 @@ class System:
         out = np.empty((self.n, 3)) if out is None else out
         check(self._lib.mdg_get_forces(self._h, out.ctypes.data, HOST))
         return out
+
+    def pme_config_batch(self, grids, order, beta):
+        g = np.ascontiguousarray(np.broadcast_to(np.asarray(grids, dtype=np.int32),
+                                                 (self.n_systems, 3)))
+        check(self._lib.mdg_pme_config_batch(self._h, g.ctypes.data_as(_c_int_p), int(order),
+                                             float(beta)))
+
+    def get_energies_batch(self):
+        """(n_systems, NUM_TERMS) energies and (n_systems,) kinetic energies."""
+        e = np.zeros((self.n_systems, NUM_TERMS))
+        ke = np.zeros(self.n_systems)
+        check(self._lib.mdg_get_energies_batch(self._h, _dp(e), _dp(ke)))
+        return e, ke
 
     def get_energies(self):
         e = np.zeros(NUM_TERMS)

@@ -94,6 +94,43 @@ int validate_box(const double *box, double cutoff) {
     return MDG_OK;
 }
 
+int validate_boxes(mdg_system *s, double cutoff) {
+    for (const SysDev &d : s->sys_h) {
+        const int rc = validate_box(d.Ld, cutoff);
+        if (rc) return rc;
+    }
+    return MDG_OK;
+}
+
+void set_sys_box(SysDev &d, const double *box) {
+    for (int k = 0; k < 3; ++k) {
+        d.Ld[k] = box[k];
+        d.L[k] = (float)box[k];
+        d.invL[k] = (float)(1.0 / box[k]);
+    }
+}
+
+double coulomb_k() {
+    // k_e = 1/(4 pi eps0) from mdpy's constants (mdpy/unit/__init__.py:56-58)
+    const double eps0 = 8.85418e-12 * 1.66053904e-27 / (1.602176634e-19 * 1.602176634e-19);
+    return 1.0 / (4.0 * 3.14159265358979323846 * eps0);
+}
+
+// FP64 Ewald self and net-charge energies of every system (depend on the
+// charges, beta and the box volume)
+void ewald_constants(mdg_system *s) {
+    const double ke = coulomb_k(), pi = 3.14159265358979323846, b = s->pme.beta;
+    s->e_self.assign(s->n_sys, 0.0);
+    s->e_net.assign(s->n_sys, 0.0);
+    if (!(b > 0)) return;
+    for (int q = 0; q < s->n_sys; ++q) {
+        const double *L = s->sys_h[q].Ld;
+        const double V = L[0] * L[1] * L[2];
+        s->e_self[q] = -ke * b / std::sqrt(pi) * s->q2sum[q];
+        s->e_net[q] = -ke * pi * s->qsum[q] * s->qsum[q] / (2.0 * b * b * V);
+    }
+}
+
 int read_status(mdg_system *s) {
     int st = 0;
     CK(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
@@ -123,19 +160,34 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
         s->steps_since_reorder = 0;
     }
     if (energy) {
-        CK(cudaMemsetAsync(s->energy, 0, sizeof(long long) * kEnergySlots, s->stream), "memset");
+        CK(cudaMemsetAsync(s->energy, 0, sizeof(long long) * kEnergySlots * s->n_sys, s->stream),
+           "memset");
         CK(cudaMemsetAsync(s->stats, 0, sizeof(unsigned long long) * 4, s->stream), "memset");
     }
     CK(launch_pack(s), "pack");
-    CK(launch_nonbonded(s, mask, energy, 0), "nonbonded");
-    CK(launch_special(s, mask, energy, 0), "special pairs");
+    // fork: PME, special pairs and bonded terms run on the side stream while
+    // the pair kernel runs on the main stream (all accumulate through
+    // order-independent fixed-point atomics); join before anything reads f
+    CK(cudaEventRecord(s->ev_fork, s->stream), "fork");
+    CK(cudaStreamWaitEvent(s->side_stream, s->ev_fork, 0), "fork wait");
+    cudaStream_t main = s->stream;
+    s->stream = s->side_stream;
+    int rc = MDG_OK;
+    cudaError_t e = cudaSuccess;
     if ((mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on) {
         int cr = 0;
-        cudaError_t e = launch_pme(s, energy, &cr);
-        if (cr != CUFFT_SUCCESS) return fail(MDG_ERR_CUFFT, "cuFFT execution failed (%d)", cr);
-        CK(e, "pme");
+        e = launch_pme(s, energy, &cr);
+        if (cr != CUFFT_SUCCESS) rc = fail(MDG_ERR_CUFFT, "cuFFT execution failed (%d)", cr);
     }
-    CK(launch_bonded(s, mask, energy), "bonded");
+    if (!rc && e == cudaSuccess) e = launch_special(s, mask, energy, 0);
+    if (!rc && e == cudaSuccess) e = launch_bonded(s, mask, energy);
+    cudaError_t ej = cudaEventRecord(s->ev_join, s->side_stream);
+    s->stream = main;
+    if (rc) return rc;
+    CK(e, "side-stream terms");
+    CK(ej, "join");
+    CK(launch_nonbonded(s, mask, energy, 0), "nonbonded");
+    CK(cudaStreamWaitEvent(s->stream, s->ev_join, 0), "join wait");
     s->evaluated_once = 1;
     return MDG_OK;
 }
@@ -211,24 +263,61 @@ MDG_API int mdg_version(int *major, int *minor) {
 MDG_API const char *mdg_last_error(void) { return g_last_error.c_str(); }
 
 MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_system **out) {
+    return mdg_system_create_batch(device, 1, &n_atoms, box, out);
+}
+
+MDG_API int mdg_system_create_batch(int device, int n_systems, const int *n_atoms,
+                                    const double *boxes, mdg_system **out) {
     if (!out) return fail(MDG_ERR_INVALID, "out is null");
     *out = nullptr;
-    if (n_atoms <= 0 || n_atoms > (1 << 26)) return fail(MDG_ERR_INVALID, "n_atoms %d out of range", n_atoms);
-    if (!box) return fail(MDG_ERR_INVALID, "box is null");
-    int rc = validate_box(box, 0.0);
-    if (rc) return rc;
+    if (n_systems < 1 || n_systems > 65536)
+        return fail(MDG_ERR_INVALID, "n_systems %d out of range", n_systems);
+    if (!n_atoms || !boxes) return fail(MDG_ERR_INVALID, "n_atoms or boxes is null");
+    long long total = 0;
+    for (int q = 0; q < n_systems; ++q) {
+        if (n_atoms[q] <= 0 || n_atoms[q] > (1 << 26))
+            return fail(MDG_ERR_INVALID, "n_atoms %d of system %d out of range", n_atoms[q], q);
+        total += n_atoms[q];
+        int rc = validate_box(boxes + 3 * q, 0.0);
+        if (rc) return rc;
+    }
+    if (total > (1 << 26)) return fail(MDG_ERR_INVALID, "%lld atoms in total: too many", total);
     CK(cudaSetDevice(device), "cudaSetDevice");
     mdg_system *s = new mdg_system();
     s->device = device;
-    s->n = n_atoms;
-    for (int d = 0; d < 3; ++d) s->box[d] = box[d];
+    s->n = (int)total;
+    s->n_sys = n_systems;
+    s->sys_h.assign(n_systems, SysDev{});
+    s->atoms_per_sys.assign(n_atoms, n_atoms + n_systems);
+    s->qsum.assign(n_systems, 0.0);
+    s->q2sum.assign(n_systems, 0.0);
+    s->e_self.assign(n_systems, 0.0);
+    s->e_net.assign(n_systems, 0.0);
+    std::vector<int> atom_sys(total);
+    int off = 0;
+    for (int q = 0; q < n_systems; ++q) {
+        SysDev &d = s->sys_h[q];
+        set_sys_box(d, boxes + 3 * q);
+        d.atom_off = off;
+        d.n_atoms = n_atoms[q];
+        std::fill(atom_sys.begin() + off, atom_sys.begin() + off + n_atoms[q], q);
+        off += n_atoms[q];
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete s;
         return cuda_fail(e, "cudaStreamCreate");
     }
     s->stream = s->own_stream;
+    e = cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        mdg_system_destroy(s);
+        return cuda_fail(e, "side stream");
+    }
     const int n = s->n;
+    int rc = MDG_OK;
 #define AL(ptr, cnt)                     \
     if ((rc = dalloc(&(ptr), (cnt)))) { \
         mdg_system_destroy(s);          \
@@ -241,9 +330,10 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
     AL(s->inv_perm, n);
     AL(s->atom_key, n);
     AL(s->tmp_perm, n);
+    AL(s->atom_sys, n);
     AL(s->x, 3 * (size_t)n);
     AL(s->v, 3 * (size_t)n);
-    AL(s->energy, kEnergySlots);
+    AL(s->energy, (size_t)kEnergySlots * n_systems);
     AL(s->status, 1);
     AL(s->stats, 4);
     AL(s->step_dev, 1);
@@ -251,12 +341,13 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
     AL(s->dump_count, 1);
     AL(s->partners, 1);
 #undef AL
-    cudaMemset(s->energy, 0, sizeof(long long) * kEnergySlots);
+    cudaMemset(s->energy, 0, sizeof(long long) * kEnergySlots * n_systems);
     cudaMemset(s->status, 0, sizeof(int));
     cudaMemset(s->step_dev, 0, sizeof(unsigned long long));
     cudaMemset(s->v, 0, sizeof(double) * 3 * n);
     cudaMemset(s->lj, 0, sizeof(float4) * n);
     cudaMemset(s->charge, 0, sizeof(float) * n);
+    cudaMemcpy(s->atom_sys, atom_sys.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
     // masses default to 1 (inv 1) so kinetic terms are defined before set_masses
     std::vector<double> ones(n, 1.0);
     cudaMemcpy(s->mass, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
@@ -273,6 +364,12 @@ MDG_API int mdg_system_create(int device, int n_atoms, const double *box, mdg_sy
         return cuda_fail(e, "system create");
     }
     *out = s;
+    return MDG_OK;
+}
+
+MDG_API int mdg_num_systems(mdg_system *s, int *n_systems) {
+    if (!s || !n_systems) return fail(MDG_ERR_INVALID, "null argument");
+    *n_systems = s->n_sys;
     return MDG_OK;
 }
 
@@ -301,6 +398,10 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->cell_cursor);
     dfree(s->atom_key);
     dfree(s->tmp_perm);
+    dfree(s->atom_sys);
+    dfree(s->cl_sys);
+    dfree(s->col_sys);
+    dfree(s->sys_dev);
     dfree(s->scan_blocks);
     dfree(s->col_ncl);
     dfree(s->col_cl_start);
@@ -323,6 +424,12 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->dih_prm);
     dfree(s->imp_idx);
     dfree(s->imp_prm);
+    if (s->side_stream) {
+        cudaStreamSynchronize(s->side_stream);
+        cudaStreamDestroy(s->side_stream);
+    }
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     return MDG_OK;
@@ -341,15 +448,30 @@ MDG_API int mdg_system_set_box(mdg_system *s, const double *box) {
     int rc = check_sys(s);
     if (rc) return rc;
     if (!box) return fail(MDG_ERR_INVALID, "box is null");
-    rc = validate_box(box, s->nb_configured ? s->cutoff : 0.0);
+    std::vector<double> all(3 * (size_t)s->n_sys);
+    for (int q = 0; q < s->n_sys; ++q) std::copy(box, box + 3, all.begin() + 3 * q);
+    return mdg_system_set_boxes(s, all.data());
+}
+
+MDG_API int mdg_system_set_boxes(mdg_system *s, const double *boxes) {
+    int rc = check_sys(s);
     if (rc) return rc;
+    if (!boxes) return fail(MDG_ERR_INVALID, "boxes is null");
+    for (int q = 0; q < s->n_sys; ++q) {
+        rc = validate_box(boxes + 3 * q, s->nb_configured ? s->cutoff : 0.0);
+        if (rc) return rc;
+    }
     CK(cudaStreamSynchronize(s->stream), "synchronize");
-    for (int d = 0; d < 3; ++d) s->box[d] = box[d];
+    for (int q = 0; q < s->n_sys; ++q) set_sys_box(s->sys_h[q], boxes + 3 * q);
     rc = prepare_sort_grid(s);
     if (rc) return fail(rc, "sort grid allocation failed");
     if (s->pme.on) {
-        rc = pme_setup(s);
+        std::vector<int> grids(3 * (size_t)s->n_sys);
+        for (int q = 0; q < s->n_sys; ++q)
+            for (int d = 0; d < 3; ++d) grids[3 * q + d] = s->sys_h[q].K[d];
+        rc = pme_setup(s, grids.data());
         if (rc) return fail(rc, "PME set-up failed");
+        ewald_constants(s);
     }
     s->need_reorder = 1;
     s->forces_valid = 0;
@@ -371,33 +493,29 @@ MDG_API int mdg_set_masses(mdg_system *s, const double *m) {
     return MDG_OK;
 }
 
-MDG_API int mdg_set_charges(mdg_system *s, const double *q) {
+MDG_API int mdg_set_charges(mdg_system *s, const double *q_in) {
     int rc = check_sys(s);
     if (rc) return rc;
-    // q * sqrt(k_e): k_e = 1/(4 pi eps0) from mdpy's constants (mdpy/unit/__init__.py:56-58)
-    const double eps0 = 8.85418e-12 * 1.66053904e-27 / (1.602176634e-19 * 1.602176634e-19);
-    const double ke = 1.0 / (4.0 * 3.14159265358979323846 * eps0);
-    const double sk = std::sqrt(ke);
+    // q * sqrt(k_e), k_e = 1/(4 pi eps0) from mdpy's constants
+    const double sk = std::sqrt(coulomb_k());
     std::vector<float> qs(s->n);
-    double sum = 0.0, sum2 = 0.0;
-    for (int i = 0; i < s->n; ++i) {
-        qs[i] = (float)(q[i] * sk);
-        sum += q[i];
-        sum2 += q[i] * q[i];
+    for (int q = 0; q < s->n_sys; ++q) {
+        const SysDev &d = s->sys_h[q];
+        double sum = 0.0, sum2 = 0.0;
+        for (int i = d.atom_off; i < d.atom_off + d.n_atoms; ++i) {
+            qs[i] = (float)(q_in[i] * sk);
+            sum += q_in[i];
+            sum2 += q_in[i] * q_in[i];
+        }
+        s->qsum[q] = sum;
+        s->q2sum[q] = sum2;
     }
     CK(cudaMemcpy(s->charge, qs.data(), sizeof(float) * s->n, cudaMemcpyHostToDevice), "copy");
     s->have_charges = 1;
     s->need_reorder = 1;
     s->forces_valid = 0;
     drop_graph(s);
-    // FP64 Ewald constants depend on the charges
-    s->pme.e_self = 0.0;
-    s->pme.e_net = 0.0;
-    if (s->pme.beta > 0) {
-        const double V = s->box[0] * s->box[1] * s->box[2];
-        s->pme.e_self = -ke * s->pme.beta / std::sqrt(3.14159265358979323846) * sum2;
-        s->pme.e_net = -ke * 3.14159265358979323846 * sum * sum / (2.0 * s->pme.beta * s->pme.beta * V);
-    }
+    ewald_constants(s);  // the FP64 Ewald constants depend on the charges
     return MDG_OK;
 }
 
@@ -427,9 +545,13 @@ MDG_API int mdg_set_exclusions(mdg_system *s, const int32_t *bonded, int bw,
     if (bw < 0 || sw < 0) return fail(MDG_ERR_INVALID, "negative width");
     // symmetric partner sets; a pair listed as both 1-2/1-3 and 1-4 stays excluded
     std::vector<std::vector<int>> excl(n), p14(n);
+    std::vector<int> sys_of(n);
+    for (int q = 0; q < s->n_sys; ++q)
+        std::fill(sys_of.begin() + s->sys_h[q].atom_off,
+                  sys_of.begin() + s->sys_h[q].atom_off + s->sys_h[q].n_atoms, q);
     auto add = [&](std::vector<std::vector<int>> &lst, int i, int j) {
         if (j < 0) return 0;
-        if (j >= n || j == i) return 1;
+        if (j >= n || j == i || sys_of[j] != sys_of[i]) return 1;
         if (std::find(lst[i].begin(), lst[i].end(), j) == lst[i].end()) lst[i].push_back(j);
         if (std::find(lst[j].begin(), lst[j].end(), i) == lst[j].end()) lst[j].push_back(i);
         return 0;
@@ -492,7 +614,7 @@ MDG_API int mdg_nonbonded_config(mdg_system *s, double cutoff, double switch_rad
     if (coulomb_mode < MDG_COUL_NONE || coulomb_mode > MDG_COUL_BARE)
         return fail(MDG_ERR_INVALID, "unknown coulomb mode %d", coulomb_mode);
     if (!(cutoff > 0)) return fail(MDG_ERR_CUTOFF, "cutoff must be positive");
-    rc = validate_box(s->box, cutoff);
+    rc = validate_boxes(s, cutoff);
     if (rc) return rc;
     if (coulomb_mode == MDG_COUL_EWALD && !(beta > 0))
         return fail(MDG_ERR_INVALID, "Ewald mode needs beta > 0");
@@ -511,35 +633,31 @@ MDG_API int mdg_pme_config(mdg_system *s, const int *grid, int order, double bet
     int rc = check_sys(s);
     if (rc) return rc;
     if (!grid) return fail(MDG_ERR_INVALID, "grid is null");
+    std::vector<int> grids(3 * (size_t)s->n_sys);
+    for (int q = 0; q < s->n_sys; ++q) std::copy(grid, grid + 3, grids.begin() + 3 * q);
+    return mdg_pme_config_batch(s, grids.data(), order, beta);
+}
+
+MDG_API int mdg_pme_config_batch(mdg_system *s, const int *grids, int order, double beta) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!grids) return fail(MDG_ERR_INVALID, "grids is null");
     if (order < 4 || order > 6) return fail(MDG_ERR_INVALID, "PME order %d not in 4..6", order);
-    for (int d = 0; d < 3; ++d)
-        if (grid[d] < 2 * order || grid[d] > 1024)
-            return fail(MDG_ERR_INVALID, "PME grid %d out of range", grid[d]);
+    for (int t = 0; t < 3 * s->n_sys; ++t)
+        if (grids[t] < 2 * order || grids[t] > 1024)
+            return fail(MDG_ERR_INVALID, "PME grid %d out of range", grids[t]);
     if (!(beta > 0)) return fail(MDG_ERR_INVALID, "PME needs beta > 0");
     CK(cudaStreamSynchronize(s->stream), "synchronize");
-    for (int d = 0; d < 3; ++d) s->pme.K[d] = grid[d];
     s->pme.order = order;
     s->pme.beta = beta;
-    rc = pme_setup(s);
+    rc = pme_setup(s, grids);
     if (rc) {
         s->pme.on = 0;
+        pme_free(s);
         return fail(rc, "PME set-up failed");
     }
     s->pme.on = 1;
-    // recompute the FP64 constants with this beta
-    std::vector<float> qs(s->n);
-    CK(cudaMemcpy(qs.data(), s->charge, sizeof(float) * s->n, cudaMemcpyDeviceToHost), "copy");
-    const double eps0 = 8.85418e-12 * 1.66053904e-27 / (1.602176634e-19 * 1.602176634e-19);
-    const double ke = 1.0 / (4.0 * 3.14159265358979323846 * eps0);
-    double sum = 0, sum2 = 0;
-    for (int i = 0; i < s->n; ++i) {
-        const double q = qs[i] / std::sqrt(ke);
-        sum += q;
-        sum2 += q * q;
-    }
-    const double V = s->box[0] * s->box[1] * s->box[2];
-    s->pme.e_self = -ke * beta / std::sqrt(3.14159265358979323846) * sum2;
-    s->pme.e_net = -ke * 3.14159265358979323846 * sum * sum / (2.0 * beta * beta * V);
+    ewald_constants(s);
     s->forces_valid = 0;
     drop_graph(s);
     return MDG_OK;
@@ -561,6 +679,17 @@ static int set_terms(mdg_system *s, int n, const int32_t *idx, const double *prm
     if (n < 0) return fail(MDG_ERR_INVALID, "negative term count");
     for (int t = 0; t < n * wi; ++t)
         if (idx[t] < 0 || idx[t] >= s->n) return fail(MDG_ERR_INVALID, "term atom index out of range");
+    if (s->n_sys > 1) {
+        // a term's atoms belong to one system
+        std::vector<int> sys_of(s->n);
+        for (int q = 0; q < s->n_sys; ++q)
+            std::fill(sys_of.begin() + s->sys_h[q].atom_off,
+                      sys_of.begin() + s->sys_h[q].atom_off + s->sys_h[q].n_atoms, q);
+        for (int t = 0; t < n; ++t)
+            for (int k = 1; k < wi; ++k)
+                if (sys_of[idx[t * wi + k]] != sys_of[idx[t * wi]])
+                    return fail(MDG_ERR_INVALID, "term %d spans two systems", t);
+    }
     CK(cudaStreamSynchronize(s->stream), "synchronize");
     if (kind == 0) {
         std::vector<int2> I(n);
@@ -726,33 +855,64 @@ MDG_API int mdg_get_forces(mdg_system *s, double *f, int where) {
     return read_status(s);
 }
 
-MDG_API int mdg_get_energies(mdg_system *s, double *energies, double *kinetic) {
+MDG_API int mdg_get_energies_batch(mdg_system *s, double *energies, double *kinetic) {
     int rc = check_sys(s);
     if (rc) return rc;
-    long long e[kEnergySlots];
-    CK(cudaMemcpyAsync(e, s->energy, sizeof(e), cudaMemcpyDeviceToHost, s->stream), "copy");
+    std::vector<long long> e((size_t)kEnergySlots * s->n_sys);
+    CK(cudaMemcpyAsync(e.data(), s->energy, sizeof(long long) * e.size(), cudaMemcpyDeviceToHost,
+                       s->stream),
+       "copy");
     CK(cudaStreamSynchronize(s->stream), "synchronize");
     rc = read_status(s);
     if (rc) return rc;
-    if (energies) {
-        for (int t = 0; t < MDG_NUM_TERMS; ++t) energies[t] = (double)e[t] * kFixInv;
-        if ((s->forces_mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on)
-            energies[MDG_TERM_COUL_RECIP] += s->pme.e_self + s->pme.e_net;
+    const bool recip = (s->forces_mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on;
+    for (int q = 0; q < s->n_sys; ++q) {
+        const long long *eq = e.data() + (size_t)kEnergySlots * q;
+        if (energies) {
+            double *out = energies + (size_t)MDG_NUM_TERMS * q;
+            for (int t = 0; t < MDG_NUM_TERMS; ++t) out[t] = (double)eq[t] * kFixInv;
+            if (recip) out[MDG_TERM_COUL_RECIP] += s->e_self[q] + s->e_net[q];
+        }
+        if (kinetic) kinetic[q] = (double)eq[kSlotKinetic] * kFixInv;
     }
-    if (kinetic) *kinetic = (double)e[kSlotKinetic] * kFixInv;
+    return MDG_OK;
+}
+
+MDG_API int mdg_get_energies(mdg_system *s, double *energies, double *kinetic) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    std::vector<double> e((size_t)MDG_NUM_TERMS * s->n_sys), k(s->n_sys);
+    rc = mdg_get_energies_batch(s, e.data(), k.data());
+    if (rc) return rc;
+    if (energies)
+        for (int t = 0; t < MDG_NUM_TERMS; ++t) {
+            double a = 0.0;
+            for (int q = 0; q < s->n_sys; ++q) a += e[(size_t)MDG_NUM_TERMS * q + t];
+            energies[t] = a;
+        }
+    if (kinetic) {
+        double a = 0.0;
+        for (int q = 0; q < s->n_sys; ++q) a += k[q];
+        *kinetic = a;
+    }
     return MDG_OK;
 }
 
 MDG_API int mdg_kinetic_energy(mdg_system *s, double *kinetic) {
     int rc = check_sys(s);
     if (rc) return rc;
-    CK(cudaMemsetAsync(s->energy + kSlotKinetic, 0, sizeof(long long), s->stream), "memset");
+    CK(cudaMemset2DAsync(s->energy + kSlotKinetic, sizeof(long long) * kEnergySlots, 0,
+                         sizeof(long long), s->n_sys, s->stream),
+       "memset");
     CK(launch_kinetic(s), "kinetic");
-    long long e = 0;
-    CK(cudaMemcpyAsync(&e, s->energy + kSlotKinetic, sizeof(e), cudaMemcpyDeviceToHost, s->stream),
+    std::vector<long long> e((size_t)kEnergySlots * s->n_sys);
+    CK(cudaMemcpyAsync(e.data(), s->energy, sizeof(long long) * e.size(), cudaMemcpyDeviceToHost,
+                       s->stream),
        "copy");
     CK(cudaStreamSynchronize(s->stream), "synchronize");
-    if (kinetic) *kinetic = (double)e * kFixInv;
+    double a = 0.0;
+    for (int q = 0; q < s->n_sys; ++q) a += (double)e[(size_t)kEnergySlots * q + kSlotKinetic] * kFixInv;
+    if (kinetic) *kinetic = a;
     return MDG_OK;
 }
 

@@ -27,7 +27,8 @@ namespace {
 struct BdArgs {
     const double *__restrict__ x;
     const int *__restrict__ inv_perm;
-    double L[3];
+    const SysDev *__restrict__ sys;
+    const int *__restrict__ atom_sys;
     const int2 *__restrict__ bidx;
     const float2 *__restrict__ bprm;
     const int4 *__restrict__ aidx;
@@ -45,11 +46,12 @@ struct BdArgs {
 };
 
 __device__ __forceinline__ float3 mind(const BdArgs &a, int i, int j) {
+    const double *L = a.sys[a.atom_sys[i]].Ld;  // a term never spans two systems
     double d[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         d[k] = a.x[3 * j + k] - a.x[3 * i + k];
-        d[k] -= a.L[k] * rint(d[k] / a.L[k]);
+        d[k] -= L[k] * rint(d[k] / L[k]);
     }
     return make_float3((float)d[0], (float)d[1], (float)d[2]);
 }
@@ -92,8 +94,10 @@ __global__ void __launch_bounds__(256) k_bonded(BdArgs a) {
     while (seg < 3 && b >= a.blk[seg + 1]) ++seg;
     const int t = (b - a.blk[seg]) * blockDim.x + threadIdx.x;
     float e = 0.f;
+    int first = -1;  // first atom of this thread's term
     if (seg == 0 && t < a.nb) {
         const int2 id = a.bidx[t];
+        first = id.x;
         const float2 p = a.bprm[t];
         const float3 d = mind(a, id.x, id.y);
         const float r = sqrtf(dot(d, d));
@@ -104,6 +108,7 @@ __global__ void __launch_bounds__(256) k_bonded(BdArgs a) {
         addf(a, id.y, -fr * d.x, -fr * d.y, -fr * d.z);
     } else if (seg == 1 && t < a.na) {
         const int4 id = a.aidx[t];
+        first = id.x;
         const float4 p = a.aprm[t];
         const float3 u = mind(a, id.y, id.x), w = mind(a, id.y, id.z);  // r21, r23
         const float lu = sqrtf(dot(u, u)), lw = sqrtf(dot(w, w));
@@ -141,6 +146,7 @@ __global__ void __launch_bounds__(256) k_bonded(BdArgs a) {
         addf(a, id.z, fl.x, fl.y, fl.z);
     } else if ((seg == 2 && t < a.nd) || (seg == 3 && t < a.ni)) {
         const int4 id = seg == 2 ? a.didx[t] : a.iidx[t];
+        first = id.x;
         float3 g[4];
         bool ok;
         const float phi = torsion(a, id, g, ok);
@@ -166,16 +172,9 @@ __global__ void __launch_bounds__(256) k_bonded(BdArgs a) {
             addf(a, id.w, -dv * g[3].x, -dv * g[3].y, -dv * g[3].z);
         }
     }
-    __shared__ double s_e[8];
-    const double d = warp_sum_d((double)e);
-    if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = d;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int w = 0; w < 8; ++w) tot += s_e[w];
-        const int term = MDG_TERM_BOND + seg;
-        fix_red((unsigned long long *)&a.energy[term], to_fix_d(tot));
-    }
+    const double v[1] = {(double)e};
+    const int slot[1] = {MDG_TERM_BOND + seg};
+    block_energy_add<1>(a.energy, first >= 0 ? a.atom_sys[first] : -1, v, slot);
 }
 
 }  // namespace
@@ -185,7 +184,8 @@ cudaError_t launch_bonded(mdg_system *s, unsigned mask, int energy) {
     BdArgs a;
     a.x = s->x;
     a.inv_perm = s->inv_perm;
-    for (int k = 0; k < 3; ++k) a.L[k] = s->box[k];
+    a.sys = s->sys_dev;
+    a.atom_sys = s->atom_sys;
     a.bidx = s->bond_idx;
     a.bprm = s->bond_prm;
     a.aidx = s->angle_idx;

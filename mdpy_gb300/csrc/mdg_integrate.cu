@@ -62,6 +62,7 @@ struct InArgs {
     unsigned long long *step;
     long long *energy;
     int *status;
+    const int *__restrict__ atom_sys;
 };
 
 __device__ __forceinline__ double fget(const unsigned long long *f, int k) {
@@ -115,22 +116,23 @@ __global__ void __launch_bounds__(256) k_post(InArgs a) {
     }
     if (i == 0) *a.step += 1ull;
     if (ENERGY) {
-        ke = warp_sum_d(ke);
-        if ((threadIdx.x & 31) == 0 && ke != 0.0)
-            fix_red((unsigned long long *)&a.energy[kSlotKinetic], to_fix_d(ke));
+        const double v[1] = {ke};
+        const int slot[1] = {kSlotKinetic};
+        block_energy_add<1>(a.energy, i < a.n ? a.atom_sys[i] : -1, v, slot);
     }
 }
 
 __global__ void __launch_bounds__(256) k_kinetic(const double *__restrict__ v,
                                                  const double *__restrict__ mass, int n,
+                                                 const int *__restrict__ atom_sys,
                                                  long long *__restrict__ energy) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double ke = 0.0;
     if (i < n) ke = 0.5 * mass[i] * (v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] +
                                      v[3 * i + 2] * v[3 * i + 2]);
-    ke = warp_sum_d(ke);
-    if ((threadIdx.x & 31) == 0 && ke != 0.0)
-        fix_red((unsigned long long *)&energy[kSlotKinetic], to_fix_d(ke));
+    const double e[1] = {ke};
+    const int slot[1] = {kSlotKinetic};
+    block_energy_add<1>(energy, i < n ? atom_sys[i] : -1, e, slot);
 }
 
 __global__ void k_forces_out(const unsigned long long *__restrict__ f,
@@ -147,11 +149,12 @@ __global__ void k_forces_out(const unsigned long long *__restrict__ f,
 // mdpy's wrap_positions (mdpy/utils/pbc.py:28-36): x - L round(x * inv) with
 // inv = float32(1/L) as mdpy stores pbc_inv (mdpy/core/state.py:53-54), so an
 // exact half-box coordinate lands on the side mdpy puts it
-__global__ void k_positions_out(const double *__restrict__ x, int n, double Lx, double Ly,
-                                double Lz, double *__restrict__ out) {
+__global__ void k_positions_out(const double *__restrict__ x, int n,
+                                const SysDev *__restrict__ sys, const int *__restrict__ atom_sys,
+                                double *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double L[3] = {Lx, Ly, Lz};
+    const double *L = sys[atom_sys[i]].Ld;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double p = x[3 * i + d];
@@ -192,6 +195,7 @@ InArgs make_args(mdg_system *s) {
     a.step = s->step_dev;
     a.energy = s->energy;
     a.status = s->status;
+    a.atom_sys = s->atom_sys;
     return a;
 }
 
@@ -215,7 +219,8 @@ cudaError_t launch_integrate_post(mdg_system *s, int energy) {
 }
 
 cudaError_t launch_kinetic(mdg_system *s) {
-    k_kinetic<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->v, s->mass, s->n, s->energy);
+    k_kinetic<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->v, s->mass, s->n, s->atom_sys,
+                                                         s->energy);
     s->launches += 1;
     return cudaGetLastError();
 }
@@ -228,8 +233,8 @@ cudaError_t launch_forces_out(mdg_system *s) {
 }
 
 cudaError_t launch_positions_out(mdg_system *s, double *out) {
-    k_positions_out<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->x, s->n, s->box[0], s->box[1],
-                                                                s->box[2], out);
+    k_positions_out<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->x, s->n, s->sys_dev,
+                                                                s->atom_sys, out);
     s->launches += 1;
     return cudaGetLastError();
 }

@@ -20,6 +20,8 @@
 #include <cufft.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/mdg.h"
 
 namespace mdg {
@@ -59,17 +61,108 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
-struct Pme {
-    int on;
+// Adds this thread's FP64 energy terms v[t] to energy[sys * kEnergySlots +
+// slot[t]] (sys < 0: nothing to add).  Every thread of the block must call it
+// (it holds a block barrier); blockDim.x is a multiple of 32.  When all
+// contributing threads belong to one system -- always, for a single system --
+// the block sums in FP64 and issues one atomic per term; a block that spans
+// systems issues one atomic per term and warp (one per lane for a warp that
+// itself spans systems).  The fixed-point sums stay order independent.
+template <int NT>
+__device__ void block_energy_add(long long *energy, int sys, const double (&v)[NT],
+                                 const int (&slot)[NT]) {
+    __shared__ double s_e[NT][32];
+    __shared__ int s_sys[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned act = __ballot_sync(0xffffffffu, sys >= 0);
+    int wsys = act ? __shfl_sync(0xffffffffu, sys, __ffs(act) - 1) : -1;
+    const bool uni = __all_sync(0xffffffffu, sys < 0 || sys == wsys);
+    double r[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) r[t] = warp_sum_d(sys >= 0 ? v[t] : 0.0);
+    if (!uni) {
+#pragma unroll
+        for (int t = 0; t < NT; ++t)
+            if (sys >= 0 && v[t] != 0.0)
+                fix_red((unsigned long long *)&energy[sys * kEnergySlots + slot[t]],
+                        to_fix_d(v[t]));
+        wsys = -1;  // added lane by lane
+    }
+    if (lane == 0) {
+        s_sys[w] = wsys;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) s_e[t][w] = r[t];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int bsys = -1;
+        bool buni = true;
+        for (int k = 0; k < nw; ++k) {
+            const int q = s_sys[k];
+            if (q < 0) continue;
+            if (bsys < 0) bsys = q;
+            else if (q != bsys) buni = false;
+        }
+        if (bsys >= 0 && buni) {
+#pragma unroll
+            for (int t = 0; t < NT; ++t) {
+                double a = 0.0;
+                for (int k = 0; k < nw; ++k)
+                    if (s_sys[k] >= 0) a += s_e[t][k];
+                if (a != 0.0)
+                    fix_red((unsigned long long *)&energy[bsys * kEnergySlots + slot[t]],
+                            to_fix_d(a));
+            }
+        } else if (!buni) {
+            for (int k = 0; k < nw; ++k) {
+                const int q = s_sys[k];
+                if (q < 0) continue;
+#pragma unroll
+                for (int t = 0; t < NT; ++t)
+                    if (s_e[t][k] != 0.0)
+                        fix_red((unsigned long long *)&energy[q * kEnergySlots + slot[t]],
+                                to_fix_d(s_e[t][k]));
+            }
+        }
+    }
+}
+
+// per-system parameters, read by kernels through a device table (one entry
+// per independent system of a batch; a single system is a batch of one)
+struct SysDev {
+    float L[3], invL[3];    // box edges (A) and inverses
+    double Ld[3];           // FP64 box for the FP64 minimum image
+    int atom_off, n_atoms;  // atom range
+    int cl_off, cl_cap;     // cluster range (capacity: ceil(n/32) + columns)
+    int col_off, n_cols;    // sort columns
+    int key_off, nzb;       // sort keys: (column, height bin)
+    int ncx, ncy;           // column grid
+    int K[3];               // PME grid
+    float kl[3];            // K / L
+    long long grid_off;     // offset of this system's real PME grid (elements)
+    long long cgrid_off;    // offset of its complex grid and influence function
+};
+
+// systems sharing one PME grid size: one batched cuFFT plan pair
+struct PmeGroup {
     int K[3];
-    int order;
-    double beta;
-    long long *grid_i;  // K0*K1*K2 fixed point charge grid
-    float *grid_r;      // real grid (FFT input, then potential)
-    float2 *grid_c;     // K0*K1*(K2/2+1)
-    float *influence;   // K0*K1*(K2/2+1)
-    cufftHandle plan_f, plan_b;
-    double e_self, e_net;  // FP64 constants of the Ewald sum
+    int count;
+    long long grid_off, cgrid_off;
+    long long nr_stride, nc_stride;  // elements between members' grids (padded)
+    cufftHandle plan_f = 0, plan_b = 0;
+    int *sys_ids = nullptr;  // device: the group's system ids, in grid order
+};
+
+struct Pme {
+    int on = 0;
+    int order = 4;
+    double beta = 0.0;
+    long long grid_total = 0, cgrid_total = 0;
+    long long *grid_i = nullptr;  // fixed-point charge grids, all systems
+    float *grid_r = nullptr;      // real grids (FFT input, then potential)
+    float2 *grid_c = nullptr;     // half-spectrum complex grids
+    float *influence = nullptr;   // influence functions, complex-grid layout
+    std::vector<PmeGroup> groups;
 };
 
 struct Graph {
@@ -82,9 +175,21 @@ struct Graph {
 
 struct mdg_system {
     int device = 0;
+    int n_sys = 1;                     // independent systems in this batch
     cudaStream_t own_stream = nullptr, stream = nullptr;
+    // side stream for the work that runs beside the pair kernel (PME, special
+    // pairs, bonded terms), joined back through two events
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int n = 0, n_pad = 0, n_clusters = 0;
-    double box[3] = {0, 0, 0};
+    std::vector<mdg::SysDev> sys_h;    // host copy of the system table
+    mdg::SysDev *sys_dev = nullptr;    // device system table
+    std::vector<int> atoms_per_sys;
+    std::vector<double> e_self, e_net; // FP64 Ewald constants per system
+    std::vector<double> qsum, q2sum;   // per-system charge sums (e)
+    int *atom_sys = nullptr;           // per atom: system id
+    int *cl_sys = nullptr;             // per cluster slot: system id
+    int *col_sys = nullptr;            // per sort column: system id
 
     // static, atom order
     double *mass = nullptr, *inv_mass = nullptr;
@@ -119,7 +224,7 @@ struct mdg_system {
     unsigned long long *f = nullptr;   // 3 * n_pad fixed point
     float4 *xq = nullptr;
     float4 *bbox = nullptr;
-    long long *energy = nullptr;       // kEnergySlots
+    long long *energy = nullptr;       // kEnergySlots per system
     int *status = nullptr;
     unsigned long long *stats = nullptr;  // 4 counters
     unsigned long long *step_dev = nullptr;
@@ -184,6 +289,7 @@ cudaError_t launch_forces_out(mdg_system *s);
 cudaError_t launch_positions_out(mdg_system *s, double *out);
 cudaError_t launch_noise(mdg_system *s, uint64_t step, float *out);
 int prepare_sort_grid(mdg_system *s);   // host: column grid + cluster-order buffers
-int pme_setup(mdg_system *s);           // host: grids, plans, influence function
+int pme_setup(mdg_system *s, const int *grids);  // host: grids, plans, influence functions
+int upload_sys_table(mdg_system *s);
 void pme_free(mdg_system *s);
 }  // namespace mdg

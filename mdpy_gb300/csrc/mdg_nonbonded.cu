@@ -55,8 +55,9 @@ struct NbArgs {
     int pw;
     const int2 *__restrict__ prange;
     const float4 *__restrict__ bbox;
+    const SysDev *__restrict__ sys;
+    const int *__restrict__ cl_sys;
     int n, n_pad, n_clusters;
-    float L[3], invL[3];
     float rc, rc2, rs2, sw_inv_den;
     float beta;
     float beta_p;        // A&S p * beta
@@ -73,11 +74,11 @@ struct NbArgs {
     const int *perm;
 };
 
-__device__ __forceinline__ void decode_shift(int code, const NbArgs &a, float &sx, float &sy,
+__device__ __forceinline__ void decode_shift(int code, const float (&L)[3], float &sx, float &sy,
                                              float &sz) {
-    sx = (float)(code / 9 - 1) * a.L[0];
-    sy = (float)((code / 3) % 3 - 1) * a.L[1];
-    sz = (float)(code % 3 - 1) * a.L[2];
+    sx = (float)(code / 9 - 1) * L[0];
+    sy = (float)((code / 3) % 3 - 1) * L[1];
+    sz = (float)(code % 3 - 1) * L[2];
 }
 
 // one j entry staged in shared memory: shifted coordinates + charge, LJ
@@ -97,6 +98,12 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
     const int part = blockIdx.x % kSplit;  // which quarter of the candidate scan
     const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
     if (cI.w == 0.f) return;  // all-padding cluster
+    // this cluster's system: its box, and the range of clusters it may pair with
+    const int sid = a.cl_sys[I];
+    const SysDev &sd = a.sys[sid];
+    const float L[3] = {sd.L[0], sd.L[1], sd.L[2]};
+    const float invL[3] = {sd.invL[0], sd.invL[1], sd.invL[2]};
+    const int cl_lo = sd.cl_off, cl_hi = sd.cl_off + sd.cl_cap;
     const int lane = threadIdx.x;
     const unsigned lt = (1u << lane) - 1u;
     const int ik = I * kCluster + lane;
@@ -209,7 +216,7 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
     // and append the survivors to this warp's ring (chunk sweeps when full)
     auto candidate = [&](int J, int code) {
         float sx, sy, sz;
-        decode_shift(code, a, sx, sy, sz);
+        decode_shift(code, L, sx, sy, sz);
         const int jk = J * kCluster + lane;
         float4 xj = a.xq[jk];
         xj.x += sx;
@@ -259,9 +266,9 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
     // split by the lane mask.  Periodic images: the nearest image of J's box
     // centre, or all 27 when a box pair spans half the box.
     unsigned n_cand = 0;
-    for (int J0 = part * 32; J0 < a.n_clusters; J0 += kSplit * 32) {
+    for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += kSplit * 32) {
         const int J = J0 + lane;
-        bool valid = J < a.n_clusters;
+        bool valid = J < cl_hi;
         if (valid && J != I) valid = ((I + J) & 1) == (I < J ? 1 : 0);
         float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
                hJ = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -276,13 +283,13 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
         bool multi = false;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            float nk = -rintf(d[k] * a.invL[k]);
+            float nk = -rintf(d[k] * invL[k]);
             nk = fminf(fmaxf(nk, -1.f), 1.f);
-            const float dd = fmaf(nk, a.L[k], d[k]);
+            const float dd = fmaf(nk, L[k], d[k]);
             const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
             g2 = fmaf(gap, gap, g2);
             ncode = ncode * 3 + (int)nk + 1;
-            multi = multi || (h[k] + a.rc >= 0.5f * a.L[k]);
+            multi = multi || (h[k] + a.rc >= 0.5f * L[k]);
         }
         valid = valid && cJ.w > 0.f;
         multi = multi && valid;
@@ -299,7 +306,7 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
                     float gg = 0.f;
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        const float dd = fmaf((float)s3[k], a.L[k], d[k]);
+                        const float dd = fmaf((float)s3[k], L[k], d[k]);
                         const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
                         gg = fmaf(gap, gap, gg);
                     }
@@ -347,8 +354,9 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
         if (lane == 0) {
             if (!(fabs(el) < kFixLimit && fabs(ee) < kFixLimit))
                 raise_status(a.status, MDG_ERR_OVERFLOW);
-            fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix_d(el));
-            fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix_d(ee));
+            long long *es = a.energy + sid * kEnergySlots;
+            fix_red((unsigned long long *)&es[MDG_TERM_LJ], to_fix_d(el));
+            fix_red((unsigned long long *)&es[MDG_TERM_COUL_REAL], to_fix_d(ee));
             atomicAdd(&a.stats[0], n_eval);
             atomicAdd(&a.stats[1], n_in);
             atomicAdd(&a.stats[2], (unsigned long long)n_cand);
@@ -363,10 +371,20 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
 __global__ void __launch_bounds__(256) k_coulomb_bare(NbArgs a) {
     __shared__ float4 s_x[256];
     // sorted slots, padding included; uncharged slots (padding has q = 0)
-    // contribute nothing and are skipped
+    // contribute nothing and are skipped; j runs over i's own system only
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const float4 xi = i < a.n_pad ? a.xq[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const bool iv = i < a.n_pad && xi.w != 0.f;
+    const int sid = i < a.n_pad ? a.cl_sys[i / kCluster] : -1;
+    float L[3] = {1.f, 1.f, 1.f}, invL[3] = {1.f, 1.f, 1.f};
+    if (sid >= 0) {
+        const SysDev &sd = a.sys[sid];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            L[k] = sd.L[k];
+            invL[k] = sd.invL[k];
+        }
+    }
     float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
     for (int base = 0; base < a.n_pad; base += 256) {
         const int jl = base + threadIdx.x;
@@ -377,6 +395,7 @@ __global__ void __launch_bounds__(256) k_coulomb_bare(NbArgs a) {
             for (int t = 0; t < lim; ++t) {
                 const int j = base + t;
                 if (j == i || s_x[t].w == 0.f) continue;
+                if (a.cl_sys[j / kCluster] != sid) continue;
                 bool excl = false;
                 for (int w = 0; w < a.pw; ++w) {
                     const int p = a.partners[(size_t)i * a.pw + w];
@@ -387,8 +406,8 @@ __global__ void __launch_bounds__(256) k_coulomb_bare(NbArgs a) {
                 float d[3] = {xj.x - xi.x, xj.y - xi.y, xj.z - xi.z};
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    const float sc = d[k] * a.invL[k];
-                    d[k] = (sc - rintf(sc)) * a.L[k];
+                    const float sc = d[k] * invL[k];
+                    d[k] = (sc - rintf(sc)) * L[k];
                 }
                 const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                 const float rinv = rsqrtf(r2);
@@ -408,15 +427,9 @@ __global__ void __launch_bounds__(256) k_coulomb_bare(NbArgs a) {
         fix_red(&a.f[a.n_pad + i], to_fix(fy));
         fix_red(&a.f[2 * a.n_pad + i], to_fix(fz));
     }
-    __shared__ float s_e[8];
-    e = warp_sum(e);
-    if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = e;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float t = 0.f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_e[w];
-        fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix(t));
-    }
+    const double v[1] = {(double)e};
+    const int slot[1] = {MDG_TERM_COUL_REAL};
+    block_energy_add<1>(a.energy, iv ? sid : -1, v, slot);
 }
 
 // ---- special pairs ---------------------------------------------------------
@@ -427,8 +440,9 @@ struct SpArgs {
     const float4 *__restrict__ lj;     // atom order
     const int2 *__restrict__ excl;
     const int2 *__restrict__ p14;
+    const SysDev *__restrict__ sys;
+    const int *__restrict__ atom_sys;
     int n_excl, n_14, n_pad;
-    double L[3];
     float rc2, rs2, sw_inv_den, beta, ewald_fc;
     int do_excl, do_lj14, do_coul14;
     unsigned long long *f;
@@ -445,15 +459,18 @@ template <bool SWITCH, bool DUMP>
 __global__ void k_special(SpArgs a) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     float e_lj = 0.f, e_cr = 0.f, e_rec = 0.f;
+    int sid = -1;
     if (t < a.n_excl + a.n_14) {
         const bool is14 = t >= a.n_excl;
         const int2 pr = is14 ? a.p14[t - a.n_excl] : a.excl[t];
         const int i = pr.x, j = pr.y;
+        sid = a.atom_sys[i];
+        const double *Ld = a.sys[sid].Ld;
         float d[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             double dd = a.x[3 * j + k] - a.x[3 * i + k];
-            dd -= a.L[k] * rint(dd / a.L[k]);
+            dd -= Ld[k] * rint(dd / Ld[k]);
             d[k] = (float)dd;
         }
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -513,27 +530,9 @@ __global__ void k_special(SpArgs a) {
     if (DUMP) return;
     // FP64 block sums: the exclusion term is a sum of O(10^5) terms of either
     // sign whose total largely cancels the self energy
-    __shared__ double s_e[3][8];
-    const double d_lj = warp_sum_d((double)e_lj), d_cr = warp_sum_d((double)e_cr),
-                 d_rec = warp_sum_d((double)e_rec);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        s_e[0][w] = d_lj;
-        s_e[1][w] = d_cr;
-        s_e[2][w] = d_rec;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-            a0 += s_e[0][k];
-            a1 += s_e[1][k];
-            a2 += s_e[2][k];
-        }
-        if (a0 != 0.0) fix_red((unsigned long long *)&a.energy[MDG_TERM_LJ], to_fix_d(a0));
-        if (a1 != 0.0) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_REAL], to_fix_d(a1));
-        if (a2 != 0.0) fix_red((unsigned long long *)&a.energy[MDG_TERM_COUL_RECIP], to_fix_d(a2));
-    }
+    const double v[3] = {(double)e_lj, (double)e_cr, (double)e_rec};
+    const int slot[3] = {MDG_TERM_LJ, MDG_TERM_COUL_REAL, MDG_TERM_COUL_RECIP};
+    block_energy_add<3>(a.energy, sid, v, slot);
 }
 
 NbArgs make_args(mdg_system *s) {
@@ -547,10 +546,8 @@ NbArgs make_args(mdg_system *s) {
     a.n = s->n;
     a.n_pad = s->n_pad;
     a.n_clusters = s->n_clusters;
-    for (int k = 0; k < 3; ++k) {
-        a.L[k] = (float)s->box[k];
-        a.invL[k] = (float)(1.0 / s->box[k]);
-    }
+    a.sys = s->sys_dev;
+    a.cl_sys = s->cl_sys;
     a.rc = s->cutoff;
     a.rc2 = s->cutoff * s->cutoff;
     const double rs = s->rswitch > 0 ? s->rswitch : s->cutoff;
@@ -626,7 +623,8 @@ cudaError_t launch_special(mdg_system *s, unsigned mask, int energy, int dump) {
     a.n_excl = s->n_excl;
     a.n_14 = s->n_14;
     a.n_pad = s->n_pad;
-    for (int k = 0; k < 3; ++k) a.L[k] = s->box[k];
+    a.sys = s->sys_dev;
+    a.atom_sys = s->atom_sys;
     a.rc2 = s->cutoff * s->cutoff;
     const double rs = s->rswitch > 0 ? s->rswitch : s->cutoff;
     a.rs2 = (float)(rs * rs);

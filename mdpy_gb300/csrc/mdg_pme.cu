@@ -27,6 +27,8 @@
 namespace mdg {
 namespace {
 
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
 // th[i] = M_p(w + p - 1 - i), dth = d th / dw (same recursion as the oracle)
 template <int P>
 __device__ __forceinline__ void spline(float w, float *th, float *dth) {
@@ -59,9 +61,9 @@ __device__ __forceinline__ void spline(float w, float *th, float *dth) {
 
 struct PmeArgs {
     const float4 *__restrict__ xq;
-    int n, n_pad;
-    int K0, K1, K2;
-    float kl0, kl1, kl2;  // K/L
+    const SysDev *__restrict__ sys;
+    const int *__restrict__ cl_sys;
+    int n_pad;
     unsigned long long *grid_i;
     const float *__restrict__ phi;
     unsigned long long *f;
@@ -88,66 +90,70 @@ __global__ void __launch_bounds__(256) k_spread(PmeArgs a) {
     if (k >= a.n_pad) return;
     const float4 p = a.xq[k];
     if (p.w == 0.f) return;  // padding slot or uncharged atom
+    const SysDev &sd = a.sys[a.cl_sys[k / kCluster]];
+    const int K0 = sd.K[0], K1 = sd.K[1], K2 = sd.K[2];
     float tx[P], ty[P], tz[P], d[P];
     int gx, gy, gz;
     float w;
-    frac<P>(p.x, a.kl0, a.K0, gx, w);
+    frac<P>(p.x, sd.kl[0], K0, gx, w);
     spline<P>(w, tx, d);
-    frac<P>(p.y, a.kl1, a.K1, gy, w);
+    frac<P>(p.y, sd.kl[1], K1, gy, w);
     spline<P>(w, ty, d);
-    frac<P>(p.z, a.kl2, a.K2, gz, w);
+    frac<P>(p.z, sd.kl[2], K2, gz, w);
     spline<P>(w, tz, d);
     int iz[P];
 #pragma unroll
-    for (int c = 0; c < P; ++c) iz[c] = (gz + c) >= a.K2 ? gz + c - a.K2 : gz + c;
+    for (int c = 0; c < P; ++c) iz[c] = (gz + c) >= K2 ? gz + c - K2 : gz + c;
+    unsigned long long *grid = a.grid_i + sd.grid_off;
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-        const int ga = (gx + i) >= a.K0 ? gx + i - a.K0 : gx + i;
+        const int ga = (gx + i) >= K0 ? gx + i - K0 : gx + i;
         const float qa = p.w * tx[i];
 #pragma unroll
         for (int j = 0; j < P; ++j) {
-            const int gb = (gy + j) >= a.K1 ? gy + j - a.K1 : gy + j;
+            const int gb = (gy + j) >= K1 ? gy + j - K1 : gy + j;
             const float qab = qa * ty[j];
-            unsigned long long *row = a.grid_i + ((size_t)ga * a.K1 + gb) * a.K2;
+            unsigned long long *row = grid + ((size_t)ga * K1 + gb) * K2;
 #pragma unroll
             for (int c = 0; c < P; ++c) fix_red(&row[iz[c]], to_fix(qab * tz[c]));
         }
     }
 }
 
-__global__ void k_grid_convert(long long *__restrict__ gi, float *__restrict__ gr, int total) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_grid_convert(long long *__restrict__ gi, float *__restrict__ gr,
+                               long long total) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= total) return;
     gr[i] = __ll2float_rn(gi[i]) * (1.0f / kFixScaleF);
     gi[i] = 0;
 }
 
+// one size group: `count` complex grids starting nc elements apart (the
+// padded stride; padding carries G = 0); grid g belongs to system sys_ids[g]
 template <bool ENERGY>
 __global__ void __launch_bounds__(256) k_convolve(float2 *__restrict__ gc,
-                                                  const float *__restrict__ G, int total, int Kh,
-                                                  int K2, long long *__restrict__ energy) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float e = 0.f;
+                                                  const float *__restrict__ G, long long total,
+                                                  long long nc, int Kh, int K2,
+                                                  const int *__restrict__ sys_ids,
+                                                  long long *__restrict__ energy) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    int q = -1;
     if (i < total) {
         const float2 c = gc[i];
         const float g = G[i];
         if (ENERGY) {
-            const int kz = i % Kh;
+            const int kz = (int)((i % nc) % Kh);
             const float wgt = (kz == 0 || (2 * kz == K2)) ? 1.0f : 2.0f;
-            e = 0.5f * wgt * g * (c.x * c.x + c.y * c.y);
+            e = (double)(0.5f * wgt * g * (c.x * c.x + c.y * c.y));
+            q = sys_ids[i / nc];
         }
         gc[i] = make_float2(c.x * g, c.y * g);
     }
     if (ENERGY) {
-        __shared__ double s_e[8];
-        const double d = warp_sum_d((double)e);
-        if ((threadIdx.x & 31) == 0) s_e[threadIdx.x >> 5] = d;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < 8; ++w) t += s_e[w];
-            fix_red((unsigned long long *)&energy[MDG_TERM_COUL_RECIP], to_fix_d(t));
-        }
+        const double v[1] = {e};
+        const int slot[1] = {MDG_TERM_COUL_RECIP};
+        block_energy_add<1>(energy, q, v, slot);
     }
 }
 
@@ -157,26 +163,29 @@ __global__ void __launch_bounds__(256) k_gather(PmeArgs a) {
     if (k >= a.n_pad) return;
     const float4 p = a.xq[k];
     if (p.w == 0.f) return;  // padding slot or uncharged atom
+    const SysDev &sd = a.sys[a.cl_sys[k / kCluster]];
+    const int K0 = sd.K[0], K1 = sd.K[1], K2 = sd.K[2];
     float tx[P], ty[P], tz[P], dx[P], dy[P], dz[P];
     int gx, gy, gz;
     float w;
-    frac<P>(p.x, a.kl0, a.K0, gx, w);
+    frac<P>(p.x, sd.kl[0], K0, gx, w);
     spline<P>(w, tx, dx);
-    frac<P>(p.y, a.kl1, a.K1, gy, w);
+    frac<P>(p.y, sd.kl[1], K1, gy, w);
     spline<P>(w, ty, dy);
-    frac<P>(p.z, a.kl2, a.K2, gz, w);
+    frac<P>(p.z, sd.kl[2], K2, gz, w);
     spline<P>(w, tz, dz);
     int iz[P];
 #pragma unroll
-    for (int c = 0; c < P; ++c) iz[c] = (gz + c) >= a.K2 ? gz + c - a.K2 : gz + c;
+    for (int c = 0; c < P; ++c) iz[c] = (gz + c) >= K2 ? gz + c - K2 : gz + c;
+    const float *phi = a.phi + sd.grid_off;
     float fx = 0.f, fy = 0.f, fz = 0.f;
 #pragma unroll
     for (int i = 0; i < P; ++i) {
-        const int ga = (gx + i) >= a.K0 ? gx + i - a.K0 : gx + i;
+        const int ga = (gx + i) >= K0 ? gx + i - K0 : gx + i;
 #pragma unroll
         for (int j = 0; j < P; ++j) {
-            const int gb = (gy + j) >= a.K1 ? gy + j - a.K1 : gy + j;
-            const float *row = a.phi + ((size_t)ga * a.K1 + gb) * a.K2;
+            const int gb = (gy + j) >= K1 ? gy + j - K1 : gy + j;
+            const float *row = phi + ((size_t)ga * K1 + gb) * K2;
             float sz = 0.f, sdz = 0.f;
 #pragma unroll
             for (int c = 0; c < P; ++c) {
@@ -189,9 +198,9 @@ __global__ void __launch_bounds__(256) k_gather(PmeArgs a) {
             fz = fmaf(tx[i] * ty[j], sdz, fz);
         }
     }
-    fx *= -p.w * a.kl0;
-    fy *= -p.w * a.kl1;
-    fz *= -p.w * a.kl2;
+    fx *= -p.w * sd.kl[0];
+    fy *= -p.w * sd.kl[1];
+    fz *= -p.w * sd.kl[2];
     fix_red(&a.f[k], to_fix(fx));
     fix_red(&a.f[a.n_pad + k], to_fix(fy));
     fix_red(&a.f[2 * a.n_pad + k], to_fix(fz));
@@ -235,9 +244,12 @@ std::vector<double> bspline_moduli(int K, int P) {
 
 void pme_free(mdg_system *s) {
     Pme &p = s->pme;
-    if (p.plan_f) cufftDestroy(p.plan_f);
-    if (p.plan_b) cufftDestroy(p.plan_b);
-    p.plan_f = p.plan_b = 0;
+    for (PmeGroup &g : p.groups) {
+        if (g.plan_f) cufftDestroy(g.plan_f);
+        if (g.plan_b) cufftDestroy(g.plan_b);
+        if (g.sys_ids) cudaFree(g.sys_ids);
+    }
+    p.groups.clear();
     cudaFree(p.grid_i);
     cudaFree(p.grid_r);
     cudaFree(p.grid_c);
@@ -246,46 +258,109 @@ void pme_free(mdg_system *s) {
     p.grid_r = nullptr;
     p.grid_c = nullptr;
     p.influence = nullptr;
+    p.grid_total = p.cgrid_total = 0;
 }
 
-// grids, cuFFT plans, and the influence function (FP64 on the host, stored float)
-int pme_setup(mdg_system *s) {
+// Grids, cuFFT plans and influence functions of every system.  grids holds
+// (K0, K1, K2) per system.  Systems with the same grid share one batched plan
+// pair (a size group); the grids of a group lie back to back, so one R2C and
+// one C2R transform the whole group.  The influence function is built in FP64
+// on the host from each system's own box and stored as float.
+int pme_setup(mdg_system *s, const int *grids) {
     Pme &p = s->pme;
     pme_free(s);
-    const int K0 = p.K[0], K1 = p.K[1], K2 = p.K[2], Kh = K2 / 2 + 1;
-    const size_t nr = (size_t)K0 * K1 * K2, nc = (size_t)K0 * K1 * Kh;
-    if (cudaMalloc(&p.grid_i, nr * sizeof(long long)) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMalloc(&p.grid_r, nr * sizeof(float)) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMalloc(&p.grid_c, nc * sizeof(float2)) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMalloc(&p.influence, nc * sizeof(float)) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMemset(p.grid_i, 0, nr * sizeof(long long)) != cudaSuccess) return MDG_ERR_CUDA;
-    if (cufftPlan3d(&p.plan_f, K0, K1, K2, CUFFT_R2C) != CUFFT_SUCCESS) return MDG_ERR_CUFFT;
-    if (cufftPlan3d(&p.plan_b, K0, K1, K2, CUFFT_C2R) != CUFFT_SUCCESS) return MDG_ERR_CUFFT;
+    const int ns = s->n_sys;
+    std::vector<std::vector<int>> members;
+    std::vector<int> gk;
+    for (int q = 0; q < ns; ++q) {
+        size_t g = 0;
+        for (; g < members.size(); ++g)
+            if (gk[3 * g] == grids[3 * q] && gk[3 * g + 1] == grids[3 * q + 1] &&
+                gk[3 * g + 2] == grids[3 * q + 2])
+                break;
+        if (g == members.size()) {
+            members.emplace_back();
+            gk.insert(gk.end(), grids + 3 * q, grids + 3 * q + 3);
+        }
+        members[g].push_back(q);
+    }
+    long long roff = 0, coff = 0;
+    for (size_t g = 0; g < members.size(); ++g) {
+        PmeGroup grp;
+        for (int d = 0; d < 3; ++d) grp.K[d] = gk[3 * g + d];
+        grp.count = (int)members[g].size();
+        // every grid starts on a 256-byte boundary (cuFFT rejects misaligned
+        // pointers): member strides are rounded up, the gaps stay zero
+        const long long nr = round_up((long long)grp.K[0] * grp.K[1] * grp.K[2], 64);
+        const long long nc = round_up((long long)grp.K[0] * grp.K[1] * (grp.K[2] / 2 + 1), 32);
+        grp.nr_stride = nr;
+        grp.nc_stride = nc;
+        grp.grid_off = roff;
+        grp.cgrid_off = coff;
+        for (int m = 0; m < grp.count; ++m) {
+            SysDev &d = s->sys_h[members[g][m]];
+            for (int k = 0; k < 3; ++k) {
+                d.K[k] = grp.K[k];
+                d.kl[k] = (float)(grp.K[k] / d.Ld[k]);
+            }
+            d.grid_off = roff + m * nr;
+            d.cgrid_off = coff + m * nc;
+        }
+        roff += grp.count * nr;
+        coff += grp.count * nc;
+        p.groups.push_back(grp);
+    }
+    p.grid_total = roff;
+    p.cgrid_total = coff;
+    if (cudaMalloc(&p.grid_i, roff * sizeof(long long)) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMalloc(&p.grid_r, roff * sizeof(float)) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMalloc(&p.grid_c, coff * sizeof(float2)) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMalloc(&p.influence, coff * sizeof(float)) != cudaSuccess) return MDG_ERR_NOMEM;
+    if (cudaMemset(p.grid_i, 0, roff * sizeof(long long)) != cudaSuccess) return MDG_ERR_CUDA;
     const double pi = 3.14159265358979323846;
-    const double *L = s->box;
-    const double V = L[0] * L[1] * L[2];
-    auto m0 = bspline_moduli(K0, p.order), m1 = bspline_moduli(K1, p.order),
-         m2 = bspline_moduli(K2, p.order);
-    std::vector<float> G(nc);
     const double b2 = p.beta * p.beta;
-    for (int a = 0; a < K0; ++a) {
-        const double fa = (a <= K0 / 2 ? a : a - K0) / L[0];
-        for (int b = 0; b < K1; ++b) {
-            const double fb = (b <= K1 / 2 ? b : b - K1) / L[1];
-            for (int c = 0; c < Kh; ++c) {
-                const double fc = c / L[2];
-                const double msq = fa * fa + fb * fb + fc * fc;
-                double g = 0.0;
-                if (msq > 0)
-                    g = std::exp(-pi * pi * msq / b2) / (pi * V * msq) / (m0[a] * m1[b] * m2[c]);
-                G[((size_t)a * K1 + b) * Kh + c] = (float)g;
+    std::vector<float> G(coff);
+    for (size_t g = 0; g < members.size(); ++g) {
+        PmeGroup &grp = p.groups[g];
+        const int K0 = grp.K[0], K1 = grp.K[1], K2 = grp.K[2], Kh = K2 / 2 + 1;
+        int n[3] = {K0, K1, K2}, nh[3] = {K0, K1, Kh};
+        if (cufftPlanMany(&grp.plan_f, 3, n, n, 1, (int)grp.nr_stride, nh, 1, (int)grp.nc_stride,
+                          CUFFT_R2C, grp.count) != CUFFT_SUCCESS ||
+            cufftPlanMany(&grp.plan_b, 3, n, nh, 1, (int)grp.nc_stride, n, 1, (int)grp.nr_stride,
+                          CUFFT_C2R, grp.count) != CUFFT_SUCCESS)
+            return MDG_ERR_CUFFT;
+        if (cudaMalloc(&grp.sys_ids, sizeof(int) * grp.count) != cudaSuccess) return MDG_ERR_NOMEM;
+        if (cudaMemcpy(grp.sys_ids, members[g].data(), sizeof(int) * grp.count,
+                       cudaMemcpyHostToDevice) != cudaSuccess)
+            return MDG_ERR_CUDA;
+        auto m0 = bspline_moduli(K0, p.order), m1 = bspline_moduli(K1, p.order),
+             m2 = bspline_moduli(K2, p.order);
+        for (int q : members[g]) {
+            const SysDev &d = s->sys_h[q];
+            const double *L = d.Ld;
+            const double V = L[0] * L[1] * L[2];
+            float *Gs = G.data() + d.cgrid_off;
+            for (int a = 0; a < K0; ++a) {
+                const double fa = (a <= K0 / 2 ? a : a - K0) / L[0];
+                for (int b = 0; b < K1; ++b) {
+                    const double fb = (b <= K1 / 2 ? b : b - K1) / L[1];
+                    for (int c = 0; c < Kh; ++c) {
+                        const double fc = c / L[2];
+                        const double msq = fa * fa + fb * fb + fc * fc;
+                        double gv = 0.0;
+                        if (msq > 0)
+                            gv = std::exp(-pi * pi * msq / b2) / (pi * V * msq) /
+                                 (m0[a] * m1[b] * m2[c]);
+                        Gs[((size_t)a * K1 + b) * Kh + c] = (float)gv;
+                    }
+                }
             }
         }
     }
-    if (cudaMemcpy(p.influence, G.data(), nc * sizeof(float), cudaMemcpyHostToDevice) !=
+    if (cudaMemcpy(p.influence, G.data(), coff * sizeof(float), cudaMemcpyHostToDevice) !=
         cudaSuccess)
         return MDG_ERR_CUDA;
-    return MDG_OK;
+    return upload_sys_table(s);
 }
 
 cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
@@ -293,14 +368,9 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
     *cufft_status = CUFFT_SUCCESS;
     PmeArgs a;
     a.xq = s->xq;
-    a.n = s->n;
+    a.sys = s->sys_dev;
+    a.cl_sys = s->cl_sys;
     a.n_pad = s->n_pad;
-    a.K0 = p.K[0];
-    a.K1 = p.K[1];
-    a.K2 = p.K[2];
-    a.kl0 = (float)(p.K[0] / s->box[0]);
-    a.kl1 = (float)(p.K[1] / s->box[1]);
-    a.kl2 = (float)(p.K[2] / s->box[2]);
     a.grid_i = (unsigned long long *)p.grid_i;
     a.phi = p.grid_r;
     a.f = s->f;
@@ -312,27 +382,40 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
         case 6: k_spread<6><<<nb, tb, 0, st>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
-    const int total = p.K[0] * p.K[1] * p.K[2];
-    k_grid_convert<<<(total + tb - 1) / tb, tb, 0, st>>>(p.grid_i, p.grid_r, total);
-    cufftResult r = cufftSetStream(p.plan_f, st);
-    if (r == CUFFT_SUCCESS) r = cufftExecR2C(p.plan_f, p.grid_r, (cufftComplex *)p.grid_c);
-    if (r != CUFFT_SUCCESS) {
-        *cufft_status = r;
-        return cudaGetLastError();
+    k_grid_convert<<<(unsigned)((p.grid_total + tb - 1) / tb), tb, 0, st>>>(p.grid_i, p.grid_r,
+                                                                            p.grid_total);
+    s->launches += 2;
+    for (PmeGroup &g : p.groups) {
+        cufftResult r = cufftSetStream(g.plan_f, st);
+        if (r == CUFFT_SUCCESS)
+            r = cufftExecR2C(g.plan_f, p.grid_r + g.grid_off, (cufftComplex *)(p.grid_c + g.cgrid_off));
+        if (r != CUFFT_SUCCESS) {
+            *cufft_status = r;
+            return cudaGetLastError();
+        }
     }
-    const int Kh = p.K[2] / 2 + 1;
-    const int totc = p.K[0] * p.K[1] * Kh;
-    if (energy)
-        k_convolve<true><<<(totc + tb - 1) / tb, tb, 0, st>>>(p.grid_c, p.influence, totc, Kh,
-                                                               p.K[2], s->energy);
-    else
-        k_convolve<false><<<(totc + tb - 1) / tb, tb, 0, st>>>(p.grid_c, p.influence, totc, Kh,
-                                                                p.K[2], s->energy);
-    r = cufftSetStream(p.plan_b, st);
-    if (r == CUFFT_SUCCESS) r = cufftExecC2R(p.plan_b, (cufftComplex *)p.grid_c, p.grid_r);
-    if (r != CUFFT_SUCCESS) {
-        *cufft_status = r;
-        return cudaGetLastError();
+    for (PmeGroup &g : p.groups) {
+        const int Kh = g.K[2] / 2 + 1;
+        const long long nc = g.nc_stride;  // padding elements carry G = 0
+        const long long totc = nc * g.count;
+        const unsigned nbc = (unsigned)((totc + tb - 1) / tb);
+        if (energy)
+            k_convolve<true><<<nbc, tb, 0, st>>>(p.grid_c + g.cgrid_off, p.influence + g.cgrid_off,
+                                                 totc, nc, Kh, g.K[2], g.sys_ids, s->energy);
+        else
+            k_convolve<false><<<nbc, tb, 0, st>>>(p.grid_c + g.cgrid_off,
+                                                  p.influence + g.cgrid_off, totc, nc, Kh, g.K[2],
+                                                  g.sys_ids, s->energy);
+        s->launches += 1;
+    }
+    for (PmeGroup &g : p.groups) {
+        cufftResult r = cufftSetStream(g.plan_b, st);
+        if (r == CUFFT_SUCCESS)
+            r = cufftExecC2R(g.plan_b, (cufftComplex *)(p.grid_c + g.cgrid_off), p.grid_r + g.grid_off);
+        if (r != CUFFT_SUCCESS) {
+            *cufft_status = r;
+            return cudaGetLastError();
+        }
     }
     switch (p.order) {
         case 4: k_gather<4><<<nb, tb, 0, st>>>(a); break;
@@ -340,7 +423,7 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
         case 6: k_gather<6><<<nb, tb, 0, st>>>(a); break;
         default: break;
     }
-    s->launches += 4;
+    s->launches += 1;
     return cudaGetLastError();
 }
 

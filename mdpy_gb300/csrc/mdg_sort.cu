@@ -31,28 +31,29 @@ namespace {
 constexpr int kScanThreads = 1024;
 constexpr int kScanPerBlock = 2 * kScanThreads;
 
-__global__ void k_bin(double *__restrict__ x, int n, double bx, double by, double bz, int ncx,
-                      int ncy, int nzb, const int *__restrict__ col_rank, int *__restrict__ key,
-                      int *__restrict__ count, int *__restrict__ status) {
+__global__ void k_bin(double *__restrict__ x, int n, const SysDev *__restrict__ sys,
+                      const int *__restrict__ atom_sys, const int *__restrict__ col_rank,
+                      int *__restrict__ key, int *__restrict__ count, int *__restrict__ status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double L[3] = {bx, by, bz};
-    const int nc[3] = {ncx, ncy, nzb};
+    const SysDev &d = sys[atom_sys[i]];
+    const int nc[3] = {d.ncx, d.ncy, d.nzb};
     int c[3];
     bool ok = true;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        double p = x[3 * i + d];
+    for (int k = 0; k < 3; ++k) {
+        const double L = d.Ld[k];
+        double p = x[3 * i + k];
         ok = ok && isfinite(p);
-        p -= L[d] * floor(p / L[d]);
-        if (p >= L[d]) p -= L[d];
+        p -= L * floor(p / L);
+        if (p >= L) p -= L;
         if (!(p >= 0.0)) p = 0.0;
-        x[3 * i + d] = p;
-        int k = (int)(p * (nc[d] / L[d]));
-        c[d] = k < 0 ? 0 : (k >= nc[d] ? nc[d] - 1 : k);
+        x[3 * i + k] = p;
+        int b = (int)(p * (nc[k] / L));
+        c[k] = b < 0 ? 0 : (b >= nc[k] ? nc[k] - 1 : b);
     }
     if (!ok) raise_status(status, MDG_ERR_PARTICLE_LOSS);
-    int k = col_rank[c[0] * ncy + c[1]] * nzb + c[2];
+    const int k = d.key_off + col_rank[d.col_off + c[0] * d.ncy + c[1]] * d.nzb + c[2];
     key[i] = k;
     atomicAdd(&count[k], 1);
 }
@@ -151,12 +152,16 @@ __global__ void k_cell_sort(const int *__restrict__ start, int ncells, int *__re
     }
 }
 
-// clusters per column (columns in rank order), then their exclusive scan
-__global__ void k_col_clusters(const int *__restrict__ start, int n_cols, int nzb,
+// clusters per column (columns of each system in rank order), then the
+// exclusive scan over all columns of all systems
+__global__ void k_col_clusters(const int *__restrict__ start, int n_cols,
+                               const SysDev *__restrict__ sys, const int *__restrict__ col_sys,
                                int *__restrict__ col_ncl) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_cols) return;
-    const int cnt = start[(c + 1) * nzb] - start[c * nzb];
+    const SysDev &d = sys[col_sys[c]];
+    const int lc = c - d.col_off;
+    const int cnt = start[d.key_off + (lc + 1) * d.nzb] - start[d.key_off + lc * d.nzb];
     col_ncl[c] = (cnt + kCluster - 1) / kCluster;
 }
 
@@ -176,9 +181,11 @@ __global__ void k_col_scan(const int *__restrict__ col_ncl, int n_cols,
     if (threadIdx.x == 0) col_cl_start[n_cols] = carry;
 }
 
-// atom of global rank g goes to its column's cluster block, in rank order
+// atom of global rank g goes to its column's cluster block, in rank order;
+// each system's clusters start at its fixed offset cl_off
 __global__ void k_finish_perm(const int *__restrict__ tmp, const int *__restrict__ key, int n,
-                              int nzb, const int *__restrict__ start,
+                              const SysDev *__restrict__ sys, const int *__restrict__ atom_sys,
+                              const int *__restrict__ start,
                               const int *__restrict__ col_cl_start, int *__restrict__ perm,
                               int *__restrict__ inv_perm, const float *__restrict__ charge,
                               const float4 *__restrict__ lj, float *__restrict__ q_sorted,
@@ -186,8 +193,11 @@ __global__ void k_finish_perm(const int *__restrict__ tmp, const int *__restrict
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
     const int i = tmp[g];
-    const int cr = key[i] / nzb;
-    const int slot = kCluster * col_cl_start[cr] + (g - start[cr * nzb]);
+    const SysDev &d = sys[atom_sys[i]];
+    const int lcr = (key[i] - d.key_off) / d.nzb;
+    const int c = d.col_off + lcr;
+    const int slot = kCluster * (d.cl_off + col_cl_start[c] - col_cl_start[d.col_off]) +
+                     (g - start[d.key_off + lcr * d.nzb]);
     perm[slot] = i;
     inv_perm[i] = slot;
     q_sorted[slot] = charge[i];
@@ -299,40 +309,52 @@ int realloc_dev(T **p, size_t count) {
 
 }  // namespace
 
-// host: column grid for this box and density, and every buffer whose size
-// depends on it (the cluster-order arrays are sized for the worst-case
-// padding: one partial cluster per column)
+// host: column grid of every system (box and density), the system table,
+// and every buffer whose size depends on them (the cluster-order arrays are
+// sized for the worst-case padding: one partial cluster per column)
 int prepare_sort_grid(mdg_system *s) {
-    const double V = s->box[0] * s->box[1] * s->box[2];
-    const double rho = std::max(s->n / V, 1e-6);
-    const double a = std::cbrt((double)kCluster / rho);
-    const int ncx = std::max(1, std::min(4096, (int)std::lround(s->box[0] / a)));
-    const int ncy = std::max(1, std::min(4096, (int)std::lround(s->box[1] / a)));
-    const int nzb = std::max(1, std::min(8192, (int)std::lround(s->box[2] / (a / 8.0))));
-    const int n_cols = ncx * ncy;
-    const long long n_keys = (long long)n_cols * nzb;
-    if (n_keys > (1ll << 26)) return MDG_ERR_INVALID;
-    s->ncell[0] = ncx;
-    s->ncell[1] = ncy;
-    s->ncell[2] = nzb;
-    s->n_cols = n_cols;
-    s->n_cells = (int)n_keys;
-    std::vector<std::pair<unsigned, int>> codes(n_cols);
-    for (int cx = 0; cx < ncx; ++cx)
-        for (int cy = 0; cy < ncy; ++cy)
-            codes[cx * ncy + cy] = {spread2(cx) | (spread2(cy) << 1), cx * ncy + cy};
-    std::sort(codes.begin(), codes.end());
-    std::vector<int> rank(n_cols);
-    for (int r = 0; r < n_cols; ++r) rank[codes[r].second] = r;
-    s->n_scan_blocks = (int)((n_keys + kScanPerBlock - 1) / kScanPerBlock);
-    const int n_clusters = (s->n + kCluster - 1) / kCluster + n_cols;
+    std::vector<int> col_rank_all, col_sys, cl_sys;
+    int col_off = 0, key_off = 0, cl_off = 0;
+    for (int q = 0; q < s->n_sys; ++q) {
+        SysDev &d = s->sys_h[q];
+        const double V = d.Ld[0] * d.Ld[1] * d.Ld[2];
+        const double rho = std::max(d.n_atoms / V, 1e-6);
+        const double a = std::cbrt((double)kCluster / rho);
+        d.ncx = std::max(1, std::min(4096, (int)std::lround(d.Ld[0] / a)));
+        d.ncy = std::max(1, std::min(4096, (int)std::lround(d.Ld[1] / a)));
+        d.nzb = std::max(1, std::min(8192, (int)std::lround(d.Ld[2] / (a / 8.0))));
+        d.n_cols = d.ncx * d.ncy;
+        d.col_off = col_off;
+        d.key_off = key_off;
+        d.cl_off = cl_off;
+        d.cl_cap = (d.n_atoms + kCluster - 1) / kCluster + d.n_cols;
+        std::vector<std::pair<unsigned, int>> codes(d.n_cols);
+        for (int cx = 0; cx < d.ncx; ++cx)
+            for (int cy = 0; cy < d.ncy; ++cy)
+                codes[cx * d.ncy + cy] = {spread2(cx) | (spread2(cy) << 1), cx * d.ncy + cy};
+        std::sort(codes.begin(), codes.end());
+        std::vector<int> rank(d.n_cols);
+        for (int r = 0; r < d.n_cols; ++r) rank[codes[r].second] = r;
+        col_rank_all.insert(col_rank_all.end(), rank.begin(), rank.end());
+        col_sys.insert(col_sys.end(), d.n_cols, q);
+        cl_sys.insert(cl_sys.end(), d.cl_cap, q);
+        col_off += d.n_cols;
+        if ((long long)key_off + (long long)d.n_cols * d.nzb > (1ll << 28)) return MDG_ERR_INVALID;
+        key_off += d.n_cols * d.nzb;
+        cl_off += d.cl_cap;
+    }
+    s->n_cols = col_off;
+    s->n_cells = key_off;
+    s->n_scan_blocks = (int)(((long long)key_off + kScanPerBlock - 1) / kScanPerBlock);
+    const int n_clusters = cl_off;
     const int n_pad = n_clusters * kCluster;
     int rc = MDG_OK;
-    if ((rc = realloc_dev(&s->cell_rank, n_cols)) || (rc = realloc_dev(&s->cell_count, n_keys)) ||
-        (rc = realloc_dev(&s->cell_start, n_keys + 1)) ||
-        (rc = realloc_dev(&s->cell_cursor, n_keys)) ||
+    if ((rc = realloc_dev(&s->cell_rank, col_off)) || (rc = realloc_dev(&s->cell_count, key_off)) ||
+        (rc = realloc_dev(&s->cell_start, (size_t)key_off + 1)) ||
+        (rc = realloc_dev(&s->cell_cursor, key_off)) ||
         (rc = realloc_dev(&s->scan_blocks, s->n_scan_blocks)) ||
-        (rc = realloc_dev(&s->col_ncl, n_cols)) || (rc = realloc_dev(&s->col_cl_start, n_cols + 1)))
+        (rc = realloc_dev(&s->col_ncl, col_off)) || (rc = realloc_dev(&s->col_cl_start, col_off + 1)) ||
+        (rc = realloc_dev(&s->col_sys, col_off)))
         return rc;
     if (n_pad != s->n_pad || !s->perm) {
         s->n_pad = n_pad;
@@ -342,15 +364,29 @@ int prepare_sort_grid(mdg_system *s) {
             (rc = realloc_dev(&s->f, 3 * (size_t)n_pad)) ||
             (rc = realloc_dev(&s->bbox, 2 * (size_t)n_clusters)) ||
             (rc = realloc_dev(&s->cluster_partner_range, n_clusters)) ||
+            (rc = realloc_dev(&s->cl_sys, n_clusters)) ||
             (rc = realloc_dev(&s->partners_sorted, (size_t)n_pad * std::max(s->pw, 1))))
             return rc;
         if (cudaMemset(s->f, 0, sizeof(unsigned long long) * 3 * n_pad) != cudaSuccess)
             return MDG_ERR_CUDA;
     }
-    if (cudaMemcpy(s->cell_rank, rank.data(), sizeof(int) * n_cols, cudaMemcpyHostToDevice) !=
-        cudaSuccess)
+    if (cudaMemcpy(s->cell_rank, col_rank_all.data(), sizeof(int) * col_off,
+                   cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->col_sys, col_sys.data(), sizeof(int) * col_off, cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(s->cl_sys, cl_sys.data(), sizeof(int) * n_clusters, cudaMemcpyHostToDevice) !=
+            cudaSuccess)
         return MDG_ERR_CUDA;
-    return MDG_OK;
+    return upload_sys_table(s);
+}
+
+int upload_sys_table(mdg_system *s) {
+    if (!s->sys_dev && cudaMalloc(&s->sys_dev, sizeof(SysDev) * s->n_sys) != cudaSuccess)
+        return MDG_ERR_NOMEM;
+    return cudaMemcpy(s->sys_dev, s->sys_h.data(), sizeof(SysDev) * s->n_sys,
+                      cudaMemcpyHostToDevice) == cudaSuccess
+               ? MDG_OK
+               : MDG_ERR_CUDA;
 }
 
 cudaError_t launch_reorder(mdg_system *s) {
@@ -362,22 +398,22 @@ cudaError_t launch_reorder(mdg_system *s) {
     cudaMemsetAsync(s->perm, 0xff, sizeof(int) * s->n_pad, st);
     cudaMemsetAsync(s->q_sorted, 0, sizeof(float) * s->n_pad, st);
     cudaMemsetAsync(s->prm_sorted, 0, sizeof(float2) * s->n_pad, st);
-    k_bin<<<(n + tb - 1) / tb, tb, 0, st>>>(s->x, n, s->box[0], s->box[1], s->box[2], s->ncell[0],
-                                            s->ncell[1], s->ncell[2], s->cell_rank, s->atom_key,
-                                            s->cell_count, s->status);
+    k_bin<<<(n + tb - 1) / tb, tb, 0, st>>>(s->x, n, s->sys_dev, s->atom_sys, s->cell_rank,
+                                            s->atom_key, s->cell_count, s->status);
     k_block_sums<<<s->n_scan_blocks, kScanThreads, 0, st>>>(s->cell_count, s->n_cells,
                                                             s->scan_blocks);
     k_scan_top<<<1, kScanThreads, 0, st>>>(s->scan_blocks, s->n_scan_blocks);
     k_scan_final<<<s->n_scan_blocks, kScanThreads, 0, st>>>(s->cell_count, s->n_cells,
                                                             s->scan_blocks, s->cell_start);
     k_col_clusters<<<(s->n_cols + tb - 1) / tb, tb, 0, st>>>(s->cell_start, s->n_cols,
-                                                             s->ncell[2], s->col_ncl);
+                                                             s->sys_dev, s->col_sys, s->col_ncl);
     k_col_scan<<<1, kScanThreads, 0, st>>>(s->col_ncl, s->n_cols, s->col_cl_start);
     k_scatter<<<(n + tb - 1) / tb, tb, 0, st>>>(s->atom_key, n, s->cell_start, s->cell_cursor,
                                                 s->tmp_perm);
     k_cell_sort<<<(s->n_cells + tb - 1) / tb, tb, 0, st>>>(s->cell_start, s->n_cells, s->tmp_perm);
-    k_finish_perm<<<(n + tb - 1) / tb, tb, 0, st>>>(s->tmp_perm, s->atom_key, n, s->ncell[2],
-                                                    s->cell_start, s->col_cl_start, s->perm,
+    k_finish_perm<<<(n + tb - 1) / tb, tb, 0, st>>>(s->tmp_perm, s->atom_key, n, s->sys_dev,
+                                                    s->atom_sys, s->cell_start, s->col_cl_start,
+                                                    s->perm,
                                                     s->inv_perm, s->charge, s->lj, s->q_sorted,
                                                     s->prm_sorted);
     k_partners_sorted<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, st>>>(

@@ -137,14 +137,16 @@ class Ensemble:
     """mdpy.Ensemble on the GPU.  ``device`` selects the CUDA device
     (default: $MDG_DEVICE or 0)."""
 
-    def __init__(self, topology, pbc_matrix, device=None):
+    def __init__(self, topology, pbc_matrix, device=None, _system=None):
         if not topology.is_joined:
             topology.join()
         self._topology = topology
         box = _diag_box(pbc_matrix)
         if device is None:
             device = int(os.environ.get("MDG_DEVICE", "0"))
-        self._system = _lib.System(topology.num_particles, box, device)
+        # _system: a stand-in that records the set-up (batch members)
+        self._system = _system if _system is not None else \
+            _lib.System(topology.num_particles, box, device)
         self._system.set_masses(np.asarray(topology.masses, dtype=np.float64).reshape(-1))
         self._system.set_charges(np.asarray(topology.charges, dtype=np.float64).reshape(-1))
         self._system.set_exclusions(topology.bonded_particles, topology.scaling_particles)

@@ -140,3 +140,53 @@ def test_ewald_beta_rule():
     # exp(-(beta rc)^2) = 2 tol, so erfc(beta rc) ~ 2 tol / (beta rc sqrt(pi)) < tol
     assert 1e-6 < erfc(b * 12.0) < 1e-5
     assert b == pytest.approx(0.2744, abs=1e-3)
+
+
+class _FakeBatchSystem:
+    """Records what EnsembleBatch sends to the device batch."""
+
+    def __init__(self, counts, boxes):
+        self.n = int(np.sum(counts))
+        self.n_systems = len(counts)
+        self.counts, self.boxes = np.asarray(counts), np.asarray(boxes)
+        self.calls = {}
+
+    def __getattr__(self, name):
+        if name.startswith("set_") or name.endswith("_config") or name.endswith("_batch"):
+            return lambda *a: self.calls.__setitem__(name, a)
+        raise AttributeError(name)
+
+
+def test_ensemble_batch_concatenates_member_setup(monkeypatch):
+    """Host side of a batch: member set-ups recorded, shifted to batch atom
+    indices, per-member PME grids, shared settings checked."""
+    from mdpy_gb300 import _lib, batch, constraint as C, systems
+
+    monkeypatch.setattr(_lib.System, "batch", classmethod(lambda cls, c, b, d=0: _FakeBatchSystem(c, b)))
+    ws = [systems.water_box(n, (3 * n / 0.1) ** (1 / 3), seed=k) for k, n in enumerate((300, 500))]
+    members = []
+    for w, grid in zip(ws, (24, 28)):
+        ens = batch.member(w.topology, w.pbc_matrix)
+        ens.add_constraints(C.NonbondedConstraint(w.parameters["nonbonded"], 9.0),
+                            C.PMEConstraint(grid_size=grid, real_space_cutoff=9.0),
+                            C.CharmmBondConstraint(w.parameters["bond"]))
+        ens.state.set_positions(w.positions)
+        members.append(ens)
+    b = batch.EnsembleBatch(members)
+    calls = b.system.calls
+    assert b.system.n == 2400 and list(b.system.counts) == [900, 1500]
+    idx, prm = calls["set_bonds"]
+    assert idx.shape == (600 + 1000, 2) and idx[600:].min() == 900      # second member shifted
+    excl = calls["set_exclusions"][0]
+    assert excl.shape[0] == 2400 and excl[900:][excl[900:] >= 0].min() >= 900
+    assert excl[:900].max() < 900
+    grids, order, beta = calls["pme_config_batch"]
+    assert grids.tolist() == [[24] * 3, [28] * 3] and order == 4
+    assert np.allclose(calls["set_positions"][0][900:], ws[1].positions)
+    # shared settings must agree
+    other = batch.member(ws[1].topology, ws[1].pbc_matrix)
+    other.add_constraints(C.NonbondedConstraint(ws[1].parameters["nonbonded"], 8.0),
+                          C.PMEConstraint(grid_size=28, real_space_cutoff=8.0),
+                          C.CharmmBondConstraint(ws[1].parameters["bond"]))
+    with pytest.raises(ValueError, match="disagree"):
+        batch.EnsembleBatch([members[0], other])
