@@ -168,6 +168,19 @@ MDG_API int mdg_get_energies(mdg_system *sys, double *energies, double *kinetic)
 /* Ensemble._update_kinetic_energy (mdpy/ensemble.py:63-71), FP64 */
 MDG_API int mdg_kinetic_energy(mdg_system *sys, double *kinetic);
 
+/* ---- no-allocation entry point (no reference counterpart) --------------
+ * kinetic[n_systems] (host) = each system's kinetic energy, bit for bit the
+ * per-system values mdg_kinetic_energy produces (mdg_get_energies_batch),
+ * computed without allocating device memory: the int64 accumulators live in
+ * a static device array sized for MDG_NOALLOC_MAX_SYSTEMS systems (128 KiB),
+ * zeroed by each call; a larger batch fails with MDG_ERR_INVALID.  The first
+ * call on a device looks the array's address up (cudaGetSymbolAddress) and
+ * must come before any stream capture.  All calls share the array: calls
+ * that overlap in time (other host threads, or other streams whose work
+ * overlaps) race on it. */
+#define MDG_NOALLOC_MAX_SYSTEMS 1024
+MDG_API int mdg_kinetic_energies_noalloc(mdg_system *sys, double *kinetic);
+
 /* ---- integration ------------------------------------------------------- */
 /* VerletIntegrator / LangevinIntegrator (mdpy/integrator/*.py) re-designed:
  * velocity Verlet or Groenbech-Jensen--Farago Langevin, FP64 x/v, one force

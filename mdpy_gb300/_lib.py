@@ -74,6 +74,7 @@ SIGNATURES = {
     "mdg_get_forces": [_sys_p, ctypes.c_void_p, ctypes.c_int],
     "mdg_get_energies": [_sys_p, _c_dbl_p, _c_dbl_p],
     "mdg_kinetic_energy": [_sys_p, _c_dbl_p],
+    "mdg_kinetic_energies_noalloc": [_sys_p, _c_dbl_p],
     "mdg_integrator_config": [_sys_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                               ctypes.c_double, ctypes.c_uint64],
     "mdg_integrate": [_sys_p, ctypes.c_int, ctypes.c_uint, ctypes.c_int],

@@ -916,6 +916,35 @@ MDG_API int mdg_kinetic_energy(mdg_system *s, double *kinetic) {
     return MDG_OK;
 }
 
+MDG_API int mdg_kinetic_energies_noalloc(mdg_system *s, double *kinetic) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!kinetic) return fail(MDG_ERR_INVALID, "kinetic is null");
+    if (s->n_sys > MDG_NOALLOC_MAX_SYSTEMS)
+        return fail(MDG_ERR_INVALID,
+                    "%d systems exceed the no-allocation scratch (at most %d systems)", s->n_sys,
+                    MDG_NOALLOC_MAX_SYSTEMS);
+    long long *acc = nullptr;
+    CK(noalloc_scratch(s->device, &acc), "cudaGetSymbolAddress of the scratch array");
+    // the accumulators start at zero
+    CK(cudaMemsetAsync(acc, 0, sizeof(long long) * kEnergySlots * s->n_sys, s->stream),
+       "memset");
+    CK(launch_kinetic_scratch(s, acc), "kinetic");
+    s->launches += 1;
+    // each system's int64 kinetic word, into the caller's array, converted in place
+    CK(cudaMemcpy2DAsync(kinetic, sizeof(double), acc + kSlotKinetic,
+                         sizeof(long long) * kEnergySlots, sizeof(long long), s->n_sys,
+                         cudaMemcpyDeviceToHost, s->stream),
+       "copy");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    for (int q = 0; q < s->n_sys; ++q) {
+        long long v;
+        std::memcpy(&v, &kinetic[q], sizeof(v));
+        kinetic[q] = (double)v * kFixInv;
+    }
+    return MDG_OK;
+}
+
 MDG_API int mdg_integrator_config(mdg_system *s, int kind, double dt, double temperature,
                                   double friction, uint64_t seed) {
     int rc = check_sys(s);

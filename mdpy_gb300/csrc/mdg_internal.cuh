@@ -292,4 +292,6 @@ int prepare_sort_grid(mdg_system *s);   // host: column grid + cluster-order buf
 int pme_setup(mdg_system *s, const int *grids);  // host: grids, plans, influence functions
 int upload_sys_table(mdg_system *s);
 void pme_free(mdg_system *s);
+cudaError_t noalloc_scratch(int device, long long **out);  // static scratch of the no-alloc path
+cudaError_t launch_kinetic_scratch(mdg_system *s, long long *acc);
 }  // namespace mdg
