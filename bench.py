@@ -35,7 +35,9 @@ METRIC = "ns/day & atom-steps/s on 1 GB300 at force err <=1e-4 vs FP64; plain vs
 DT_FS = 1.0
 TEMPERATURE = 300.0
 FRICTION = 0.001          # 1/ps in 1/fs
-CUTOFF, SWITCH, GRID, ORDER, EWALD_TOL = 12.0, 10.0, 96, 4, 1e-5
+CUTOFF, SWITCH, ORDER, EWALD_TOL = 12.0, 10.0, 4, 1e-5
+# single-system workloads: waters, box edge (A), chain beads, PME grid
+WORKLOADS = {"water90k": (30000, 96.5, 500, 96), "water1m": (333333, 215.0, 0, 224)}
 L2_FLUSH_BYTES = 256 << 20
 PEAKS = os.path.join(HERE, "MEASURED_PEAKS.json")
 PROFILE_INPUTS = os.path.join(HERE, "profiles", "roofline_inputs.json")
@@ -48,44 +50,65 @@ def parse():
     p.add_argument("--steps", type=int, default=3000)
     p.add_argument("--warmup", type=int, default=50)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="water90k", choices=["water90k", "batch256"],
-                   help="water90k: the 88k-atom box (default); batch256: 256 independent "
-                        "water boxes of 1.5k-12k atoms in one batch")
+    p.add_argument("--workload", default="water90k", choices=["water90k", "water1m", "batch256"],
+                   help="water90k: the 88k-atom water + chain box (default); water1m: 333,333 "
+                        "waters (1M atoms) in a 215 A box; batch256: 256 independent water "
+                        "boxes of 1.5k-12k atoms in one batch")
     p.add_argument("--boxes", type=int, default=256)
-    p.add_argument("--waters", type=int, default=30000)
-    p.add_argument("--box", type=float, default=96.5)
-    p.add_argument("--beads", type=int, default=500)
+    p.add_argument("--waters", type=int, default=None)
+    p.add_argument("--box", type=float, default=None)
+    p.add_argument("--beads", type=int, default=None)
     p.add_argument("--e2e-steps", type=int, default=100)
     p.add_argument("--kernel-reps", type=int, default=200)
     p.add_argument("--cpu-seconds", type=float, default=20.0)
     p.add_argument("--no-error-check", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    return p.parse_args()
+    p.add_argument("--nve-ps", type=float, default=None,
+                   help="velocity-Verlet NVE run after the timed region for the energy drift "
+                        "(default 100 ps on water90k, 0 elsewhere)")
+    a = p.parse_args()
+    w, b, beads, grid = WORKLOADS.get(a.workload, WORKLOADS["water90k"])
+    a.waters = w if a.waters is None else a.waters
+    a.box = b if a.box is None else a.box
+    a.beads = beads if a.beads is None else a.beads
+    a.grid = grid
+    if a.nve_ps is None:
+        a.nve_ps = 100.0 if a.workload == "water90k" else 0.0
+    if a.workload == "water1m":
+        # the FP64 references (all-pairs Coulomb, direct Ewald k-sum) do not
+        # finish at 1M atoms; the 88k-atom box carries both numbers
+        a.no_error_check = True
+        a.no_cpu_baseline = True
+    return a
 
 
 def workload_name(a, n_atoms):
     return ("water%dk_chain%d_%.1fA_%d_atoms_rc%g_sw%g_pme%d_o%d_langevin300K_1fs"
-            % (a.waters // 1000, a.beads, a.box, n_atoms, CUTOFF, SWITCH, GRID, ORDER))
+            % (a.waters // 1000, a.beads, a.box, n_atoms, CUTOFF, SWITCH, a.grid, ORDER))
 
 
 def make_system(a, seed):
     from mdpy_gb300 import systems
 
+    if a.beads == 0:
+        return systems.water_box(a.waters, a.box, seed=seed)
     return systems.chain_in_water(n_waters=a.waters, box=a.box, n_beads=a.beads, seed=seed)
 
 
-def make_ensemble(s, device):
+def make_ensemble(s, device, grid):
     from mdpy_gb300 import constraint as C
     from mdpy_gb300.ensemble import Ensemble
 
     ens = Ensemble(s.topology, s.pbc_matrix, device=device)
     nb = C.NonbondedConstraint(s.parameters["nonbonded"], cutoff_radius=CUTOFF,
                                switch_radius=SWITCH, ewald_error=EWALD_TOL)
-    pme = C.PMEConstraint(grid_size=GRID, order=ORDER, ewald_error=EWALD_TOL,
+    pme = C.PMEConstraint(grid_size=grid, order=ORDER, ewald_error=EWALD_TOL,
                           real_space_cutoff=CUTOFF)
-    ens.add_constraints(nb, pme, C.CharmmBondConstraint(s.parameters["bond"]),
-                        C.CharmmAngleConstraint(s.parameters["angle"]),
-                        C.CharmmDihedralConstraint(None, float_parameters=s.dihedral_parameters))
+    cons = [nb, pme, C.CharmmBondConstraint(s.parameters["bond"]),
+            C.CharmmAngleConstraint(s.parameters["angle"])]
+    if s.topology.num_dihedrals:
+        cons.append(C.CharmmDihedralConstraint(None, float_parameters=s.dihedral_parameters))
+    ens.add_constraints(*cons)
     ens.state.set_positions(s.positions)
     ens.state.set_velocities(s.velocities)
     return ens, nb.ewald_beta
@@ -320,6 +343,42 @@ def barrier(world):
         dist.barrier()
 
 
+def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0):
+    """Total-energy drift of a velocity-Verlet run of ``ps`` picoseconds:
+    ``equilibrate_ps`` of Langevin at 300 K first (the lattice start relaxes
+    for several ps, which shows as a spurious trend), then the least-squares
+    slope of E(t), sampled every ``chunk`` steps, in kT per ns per atom."""
+    from mdpy_gb300 import _lib, unit
+
+    sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 77 + seed)
+    sysm.integrate(int(equilibrate_ps * 1000.0 / DT_FS), mask, want_energy=False)
+    sysm.integrator_config(_lib.INTEGRATOR_VERLET, DT_FS)
+    n_chunks = max(2, int(round(ps * 1000.0 / DT_FS / chunk)))
+    terms = [t for t in range(_lib.NUM_TERMS) if mask >> t & 1]
+    t_fs, e_tot = [], []
+    t0 = time.perf_counter()
+    for k in range(n_chunks):
+        sysm.integrate(chunk, mask, want_energy=True)
+        e, ke = sysm.get_energies()
+        t_fs.append((k + 1) * chunk * DT_FS)
+        e_tot.append(float(sum(e[t] for t in terms) + ke))
+    wall = time.perf_counter() - t0
+    slope = float(np.polyfit(np.array(t_fs), np.array(e_tot), 1)[0])   # energy unit / fs
+    kT = unit.KB * TEMPERATURE
+    drift = slope * 1e6 / (n_atoms * kT)
+    e0 = e_tot[0]
+    half = n_chunks // 2
+    halves = [float(np.polyfit(np.array(t_fs[i:j]), np.array(e_tot[i:j]), 1)[0]) * 1e6
+              / (n_atoms * kT) for i, j in ((0, half), (half, n_chunks))]
+    return {"kT_per_ns_per_atom": drift, "halves_kT_per_ns_per_atom": halves,
+            "ps": n_chunks * chunk * DT_FS / 1000.0,
+            "samples": n_chunks, "sample_every_steps": chunk,
+            "max_abs_dev_kT_per_atom": float(np.max(np.abs(np.array(e_tot) - e0)) / (n_atoms * kT)),
+            "integrator": "velocity Verlet, dt 1 fs, after %g ps of Langevin at 300 K"
+                          % equilibrate_ps,
+            "wall_s": wall}
+
+
 # --------------------------------------------------------------------------
 # CPU arm: the oracle port of the reference path, on the host cores
 # --------------------------------------------------------------------------
@@ -350,7 +409,8 @@ def cpu_reference_sample(s, seconds):
                             t.scaling_particles, CUTOFF, lj=False, coulomb="bare")
         O.bonds(s.positions, s.box, t.bonds, kb)
         O.angles(s.positions, s.box, t.angles, ka)
-        O.dihedrals(s.positions, s.box, t.dihedrals, s.dihedral_parameters)
+        if t.num_dihedrals:
+            O.dihedrals(s.positions, s.box, t.dihedrals, s.dihedral_parameters)
         evals += 1
         if time.perf_counter() - t0 >= seconds or time.perf_counter() - te > seconds / 2:
             break
@@ -397,7 +457,8 @@ def force_error(s, ens, beta, n_sample=1000, seed=0):
                    for i, j, k in t.angles])
     f_b, _ = O.bonds(pos, s.box, t.bonds, kb)
     f_a, _ = O.angles(pos, s.box, t.angles, ka)
-    f_d, _ = O.dihedrals(pos, s.box, t.dihedrals, s.dihedral_parameters)
+    f_d = O.dihedrals(pos, s.box, t.dihedrals, s.dihedral_parameters)[0] \
+        if t.num_dihedrals else 0.0
     ref = (f_nb + f_ex + f_b + f_a + f_d)[sub] + f_rec
     err = float(np.sqrt(np.sum((f_gpu[sub] - ref) ** 2) / np.sum(ref ** 2)))
     return err, len(sub)
@@ -442,7 +503,7 @@ def main():
     torch.cuda.set_device(local)
     s = make_system(a, seed=rank)
     n = s.num_particles
-    ens, beta = make_ensemble(s, local)
+    ens, beta = make_ensemble(s, local, a.grid)
     sysm = ens.system
     # a dedicated stream: the library, the L2 flush and the timing events all
     # go to it (torch's default stream is the legacy stream, handle 0)
@@ -566,6 +627,8 @@ def main():
            "api": "mdg_set_positions/velocities(host) + mdg_integrate(1) + "
                   "mdg_get_positions/velocities(host) + mdg_get_energies"}
 
+    nve = nve_drift(sysm, mask, n, a.nve_ps) if a.nve_ps > 0 else None
+
     err = None
     cpu = None
     if rank == 0 and world == 1:
@@ -591,6 +654,7 @@ def main():
                        "form": "plain"},
             "atom_steps_per_s": n * sps_job,
             "force_rel_rms_err_vs_fp64": err,
+            "nve_drift": nve,
             "plain": plain, "chosen": dict(plain, form="plain"),
             "roofline": roofline, "stages_ms": stage_ms, "nonbonded_stats": stats,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),

@@ -168,6 +168,13 @@ MDG_API int mdg_get_energies(mdg_system *sys, double *energies, double *kinetic)
 /* Ensemble._update_kinetic_energy (mdpy/ensemble.py:63-71), FP64 */
 MDG_API int mdg_kinetic_energy(mdg_system *sys, double *kinetic);
 
+/* ---- energy minimisation ------------------------------------------------ */
+/* One move of SteepestDescentMinimizer.minimize
+ * (mdpy/minimizer/steepest_descent_minimizer.py:39-42): x_i += alpha F_i/|F_i|
+ * from the forces of the last evaluation (atoms with zero force stay put).
+ * The caller re-evaluates (mdg_compute_forces) and tests the energy. */
+MDG_API int mdg_minimize_step(mdg_system *sys, double alpha);
+
 /* ---- no-allocation entry point (no reference counterpart) --------------
  * kinetic[n_systems] (host) = each system's kinetic energy, bit for bit the
  * per-system values mdg_kinetic_energy produces (mdg_get_energies_batch),

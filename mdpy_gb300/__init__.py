@@ -21,11 +21,20 @@ def __getattr__(name):
     if name == "Simulation":
         from .simulation import Simulation
         return Simulation
-    if name in ("constraint", "integrator", "simulation", "ensemble", "systems", "_lib"):
+    if name in ("SteepestDescentMinimizer", "ConjugateGradientMinimizer"):
+        from . import minimizer
+        return getattr(minimizer, name)
+    if name == "EnsembleBatch":
+        from .batch import EnsembleBatch
+        return EnsembleBatch
+    if name in ("constraint", "integrator", "simulation", "ensemble", "systems", "_lib",
+                "minimizer", "batch", "forcefield"):
         import importlib
         return importlib.import_module("." + name, __name__)
     raise AttributeError(name)
 
 
 __all__ = ["unit", "error", "Particle", "Topology", "Ensemble", "State", "Simulation",
-           "constraint", "integrator", "simulation", "systems"]
+           "SteepestDescentMinimizer", "ConjugateGradientMinimizer", "EnsembleBatch",
+           "constraint", "integrator", "simulation", "systems", "minimizer", "batch",
+           "forcefield"]

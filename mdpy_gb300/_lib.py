@@ -75,6 +75,7 @@ SIGNATURES = {
     "mdg_get_energies": [_sys_p, _c_dbl_p, _c_dbl_p],
     "mdg_kinetic_energy": [_sys_p, _c_dbl_p],
     "mdg_kinetic_energies_noalloc": [_sys_p, _c_dbl_p],
+    "mdg_minimize_step": [_sys_p, ctypes.c_double],
     "mdg_integrator_config": [_sys_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                               ctypes.c_double, ctypes.c_uint64],
     "mdg_integrate": [_sys_p, ctypes.c_int, ctypes.c_uint, ctypes.c_int],
@@ -307,6 +308,9 @@ class System:
         ke = ctypes.c_double(0.0)
         check(self._lib.mdg_get_energies(self._h, _dp(e), ctypes.byref(ke)))
         return e, ke.value
+
+    def minimize_step(self, alpha):
+        check(self._lib.mdg_minimize_step(self._h, float(alpha)))
 
     def kinetic_energy(self):
         ke = ctypes.c_double(0.0)

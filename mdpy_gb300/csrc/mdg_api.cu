@@ -401,6 +401,9 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->atom_sys);
     dfree(s->cl_sys);
     dfree(s->col_sys);
+    dfree(s->cl_col);
+    dfree(s->col_xy);
+    dfree(s->overhang);
     dfree(s->sys_dev);
     dfree(s->scan_blocks);
     dfree(s->col_ncl);
@@ -942,6 +945,18 @@ MDG_API int mdg_kinetic_energies_noalloc(mdg_system *s, double *kinetic) {
         std::memcpy(&v, &kinetic[q], sizeof(v));
         kinetic[q] = (double)v * kFixInv;
     }
+    return MDG_OK;
+}
+
+MDG_API int mdg_minimize_step(mdg_system *s, double alpha) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!(alpha > 0) || !std::isfinite(alpha))
+        return fail(MDG_ERR_INVALID, "step length %g must be positive", alpha);
+    if (!s->forces_valid) return fail(MDG_ERR_STATE, "no force evaluation since the last change");
+    CK(launch_sd_step(s, alpha), "steepest-descent step");
+    s->forces_valid = 0;
+    if (++s->steps_since_reorder >= s->reorder_interval) s->need_reorder = 1;
     return MDG_OK;
 }
 

@@ -172,6 +172,32 @@ __global__ void k_noise(int n, unsigned long long step, unsigned long long seed,
     out[3 * i + 2] = g.z;
 }
 
+// one steepest-descent move (SteepestDescentMinimizer.minimize,
+// mdpy/minimizer/steepest_descent_minimizer.py:39-42): every atom moves
+// alpha A along its own force direction.  An atom with zero force stays put
+// (the reference divides by the zero norm).
+__global__ void __launch_bounds__(256) k_sd_step(double *__restrict__ x,
+                                                 const unsigned long long *__restrict__ f,
+                                                 const int *__restrict__ inv_perm, int n,
+                                                 int n_pad, double alpha,
+                                                 int *__restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int k = inv_perm[i];
+    const double F[3] = {fget(f, k), fget(f, n_pad + k), fget(f, 2 * n_pad + k)};
+    const double norm = sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+    if (!(norm > 0.0)) return;
+    const double c = alpha / norm;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double xn = x[3 * i + d] + c * F[d];
+        ok = ok && isfinite(xn);
+        x[3 * i + d] = xn;
+    }
+    if (!ok) raise_status(status, MDG_ERR_PARTICLE_LOSS);
+}
+
 InArgs make_args(mdg_system *s) {
     InArgs a;
     a.x = s->x;
@@ -235,6 +261,13 @@ cudaError_t launch_forces_out(mdg_system *s) {
 cudaError_t launch_positions_out(mdg_system *s, double *out) {
     k_positions_out<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->x, s->n, s->sys_dev,
                                                                 s->atom_sys, out);
+    s->launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sd_step(mdg_system *s, double alpha) {
+    k_sd_step<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->x, s->f, s->inv_perm, s->n, s->n_pad,
+                                                         alpha, s->status);
     s->launches += 1;
     return cudaGetLastError();
 }

@@ -137,6 +137,7 @@ struct SysDev {
     int col_off, n_cols;    // sort columns
     int key_off, nzb;       // sort keys: (column, height bin)
     int ncx, ncy;           // column grid
+    int col_mode;           // pair search over neighbouring columns (else all clusters)
     int K[3];               // PME grid
     float kl[3];            // K / L
     long long grid_off;     // offset of this system's real PME grid (elements)
@@ -190,6 +191,10 @@ struct mdg_system {
     int *atom_sys = nullptr;           // per atom: system id
     int *cl_sys = nullptr;             // per cluster slot: system id
     int *col_sys = nullptr;            // per sort column: system id
+    int *cl_col = nullptr;             // per cluster slot: global sort column (-1: none)
+    int *col_xy = nullptr;             // per global sort column: (cx << 16) | cy
+    float *overhang = nullptr;         // per system: how far (A) cluster boxes reach out
+                                       // of their columns since the last re-sort
 
     // static, atom order
     double *mass = nullptr, *inv_mass = nullptr;
@@ -288,6 +293,7 @@ cudaError_t launch_kinetic(mdg_system *s);
 cudaError_t launch_forces_out(mdg_system *s);
 cudaError_t launch_positions_out(mdg_system *s, double *out);
 cudaError_t launch_noise(mdg_system *s, uint64_t step, float *out);
+cudaError_t launch_sd_step(mdg_system *s, double alpha);
 int prepare_sort_grid(mdg_system *s);   // host: column grid + cluster-order buffers
 int pme_setup(mdg_system *s, const int *grids);  // host: grids, plans, influence functions
 int upload_sys_table(mdg_system *s);

@@ -57,6 +57,12 @@ struct NbArgs {
     const float4 *__restrict__ bbox;
     const SysDev *__restrict__ sys;
     const int *__restrict__ cl_sys;
+    const int *__restrict__ cl_col;        // cluster -> global sort column
+    const int *__restrict__ col_xy;        // global column -> (cx << 16) | cy
+    const int *__restrict__ col_rank;      // system column (cx * ncy + cy) -> rank
+    const int *__restrict__ col_cl_start;  // global column -> first cluster (scan)
+    const int *__restrict__ col_ncl;       // global column -> clusters
+    const float *__restrict__ overhang;    // per system, A
     int n, n_pad, n_clusters;
     float rc, rc2, rs2, sw_inv_den;
     float beta;
@@ -266,64 +272,157 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
     // split by the lane mask.  Periodic images: the nearest image of J's box
     // centre, or all 27 when a box pair spans half the box.
     unsigned n_cand = 0;
-    for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += kSplit * 32) {
-        const int J = J0 + lane;
-        bool valid = J < cl_hi;
-        if (valid && J != I) valid = ((I + J) & 1) == (I < J ? 1 : 0);
-        float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
-               hJ = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (valid) {
-            cJ = a.bbox[2 * J];
-            hJ = a.bbox[2 * J + 1];
+    // every lane offers one (J, image) candidate; the hits go to candidate()
+    auto offer = [&](bool hit, int J, int code) {
+        unsigned b = __ballot_sync(kFull, hit);
+        if (ENERGY) n_cand += __popc(b);
+        while (b) {
+            const int src = __ffs(b) - 1;
+            b &= b - 1;
+            candidate(__shfl_sync(kFull, J, src), __shfl_sync(kFull, code, src));
         }
-        const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
-        const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
-        int ncode = 0;
-        float g2 = 0.f;
-        bool multi = false;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float nk = -rintf(d[k] * invL[k]);
-            nk = fminf(fmaxf(nk, -1.f), 1.f);
-            const float dd = fmaf(nk, L[k], d[k]);
-            const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
-            g2 = fmaf(gap, gap, g2);
-            ncode = ncode * 3 + (int)nk + 1;
-            multi = multi || (h[k] + a.rc >= 0.5f * L[k]);
-        }
-        valid = valid && cJ.w > 0.f;
-        multi = multi && valid;
-        const bool near_hit = valid && g2 <= a.rc2;
-        const bool any_multi = __any_sync(kFull, multi);
-        const int passes = any_multi ? 27 : 1;
-        for (int pass = 0; pass < passes; ++pass) {
-            bool hit;
-            int code;
-            if (any_multi) {
-                code = pass;
-                if (multi) {
-                    const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
-                    float gg = 0.f;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const float dd = fmaf((float)s3[k], L[k], d[k]);
-                        const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
-                        gg = fmaf(gap, gap, gg);
-                    }
-                    hit = gg <= a.rc2;
-                } else {
-                    hit = near_hit && code == ncode;
-                }
-            } else {
-                code = ncode;
-                hit = near_hit;
+    };
+    // the half-shell owner rule
+    auto owned = [&](int J) { return J == I || ((I + J) & 1) == (I < J ? 1 : 0); };
+
+    // Column mode (systems whose columns span at least 2R+1 in x and y):
+    // candidates come only from the (2R+1)^2 columns around I's column, R =
+    // the column reach of rc plus twice the largest distance any cluster box
+    // has moved out of its column since the last re-sort.  Each column is a
+    // contiguous run of clusters; the runs are concatenated into one virtual
+    // list (warp scan of the run lengths) walked 32 at a time.
+    int R = 0;
+    bool colmode = sd.col_mode != 0;
+    if (colmode) {
+        const float ov = a.overhang[sid];
+        const float aw = fminf(L[0] / (float)sd.ncx, L[1] / (float)sd.ncy);
+        R = (int)floorf((a.rc + 2.f * ov) / aw) + 1;
+        colmode = 2 * R + 1 <= min(sd.ncx, sd.ncy);
+    }
+    if (colmode) {
+        const int pk = a.col_xy[a.cl_col[I]];
+        const int cx = pk >> 16, cy = pk & 0xffff;
+        const int side = 2 * R + 1, ncn = side * side;
+        const int base0 = a.col_cl_start[sd.col_off];
+        for (int cb = 0; cb < ncn; cb += 32) {
+            const int c = cb + lane;
+            int cnt = 0, start = 0, shc = 4;  // shc: (sx + 1) * 3 + (sy + 1)
+            if (c < ncn) {
+                int x2 = cx + c / side - R, y2 = cy + c % side - R;
+                const int sx = x2 < 0 ? -1 : (x2 >= sd.ncx ? 1 : 0);
+                const int sy = y2 < 0 ? -1 : (y2 >= sd.ncy ? 1 : 0);
+                x2 -= sx * sd.ncx;
+                y2 -= sy * sd.ncy;
+                const int gc = sd.col_off + a.col_rank[sd.col_off + x2 * sd.ncy + y2];
+                start = sd.cl_off + a.col_cl_start[gc] - base0;
+                cnt = a.col_ncl[gc];
+                shc = (sx + 1) * 3 + (sy + 1);
             }
-            unsigned b = __ballot_sync(kFull, hit);
-            if (ENERGY) n_cand += __popc(b);
-            while (b) {
-                const int src = __ffs(b) - 1;
-                b &= b - 1;
-                candidate(__shfl_sync(kFull, J, src), __shfl_sync(kFull, code, src));
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(kFull, incl, 31);
+            for (int v0 = part * 32; v0 < total; v0 += kSplit * 32) {
+                const int v = v0 + lane;
+                int lo = 0, hi = 31;  // first lane whose inclusive count exceeds v
+#pragma unroll
+                for (int it = 0; it < 5; ++it) {
+                    const int mid = (lo + hi) >> 1;
+                    const int im = __shfl_sync(kFull, incl, mid);
+                    if (im > v) hi = mid;
+                    else lo = mid + 1;
+                }
+                const int s_incl = __shfl_sync(kFull, incl, lo);
+                const int s_cnt = __shfl_sync(kFull, cnt, lo);
+                const int s_start = __shfl_sync(kFull, start, lo);
+                const int s_shc = __shfl_sync(kFull, shc, lo);
+                const int J = s_start + (v - (s_incl - s_cnt));
+                bool valid = v < total && owned(J);
+                float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                       hJ = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (valid) {
+                    cJ = a.bbox[2 * J];
+                    hJ = a.bbox[2 * J + 1];
+                }
+                valid = valid && cJ.w > 0.f;
+                // x and y images follow from the column wrap; z takes the
+                // nearest image of the box centres, or all three when a box
+                // pair spans half the box height
+                const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+                const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+                const float gx = fmaxf(fabsf(fmaf((float)(s_shc / 3 - 1), L[0], d[0])) - h[0], 0.f);
+                const float gy = fmaxf(fabsf(fmaf((float)(s_shc % 3 - 1), L[1], d[1])) - h[1], 0.f);
+                const float gxy = fmaf(gx, gx, gy * gy);
+                float nz = -rintf(d[2] * invL[2]);
+                nz = fminf(fmaxf(nz, -1.f), 1.f);
+                const float gz = fmaxf(fabsf(fmaf(nz, L[2], d[2])) - h[2], 0.f);
+                const bool near_hit = valid && fmaf(gz, gz, gxy) <= a.rc2;
+                const bool multi_z = valid && (h[2] + a.rc >= 0.5f * L[2]);
+                if (!__any_sync(kFull, multi_z)) {
+                    offer(near_hit, J, s_shc * 3 + (int)nz + 1);
+                } else {
+                    for (int zz = -1; zz <= 1; ++zz) {
+                        bool hit = near_hit && zz == (int)nz;
+                        if (multi_z) {
+                            const float g = fmaxf(fabsf(fmaf((float)zz, L[2], d[2])) - h[2], 0.f);
+                            hit = fmaf(g, g, gxy) <= a.rc2;
+                        }
+                        offer(hit, J, s_shc * 3 + zz + 1);
+                    }
+                }
+            }
+        }
+    } else {
+        // full scan of the system's clusters: work item `part` takes batches
+        // part, part + kSplit, ... of 32 clusters
+        for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += kSplit * 32) {
+            const int J = J0 + lane;
+            bool valid = J < cl_hi && owned(J);
+            float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                   hJ = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) {
+                cJ = a.bbox[2 * J];
+                hJ = a.bbox[2 * J + 1];
+            }
+            const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+            const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+            int ncode = 0;
+            float g2 = 0.f;
+            bool multi = false;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float nk = -rintf(d[k] * invL[k]);
+                nk = fminf(fmaxf(nk, -1.f), 1.f);
+                const float dd = fmaf(nk, L[k], d[k]);
+                const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                g2 = fmaf(gap, gap, g2);
+                ncode = ncode * 3 + (int)nk + 1;
+                multi = multi || (h[k] + a.rc >= 0.5f * L[k]);
+            }
+            valid = valid && cJ.w > 0.f;
+            multi = multi && valid;
+            const bool near_hit = valid && g2 <= a.rc2;
+            if (!__any_sync(kFull, multi)) {
+                offer(near_hit, J, ncode);
+            } else {
+                for (int code = 0; code < 27; ++code) {
+                    bool hit = near_hit && code == ncode;
+                    if (multi) {
+                        const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
+                        float gg = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            const float dd = fmaf((float)s3[k], L[k], d[k]);
+                            const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                            gg = fmaf(gap, gap, gg);
+                        }
+                        hit = gg <= a.rc2;
+                    }
+                    offer(hit, J, code);
+                }
             }
         }
     }
@@ -548,6 +647,12 @@ NbArgs make_args(mdg_system *s) {
     a.n_clusters = s->n_clusters;
     a.sys = s->sys_dev;
     a.cl_sys = s->cl_sys;
+    a.cl_col = s->cl_col;
+    a.col_xy = s->col_xy;
+    a.col_rank = s->cell_rank;
+    a.col_cl_start = s->col_cl_start;
+    a.col_ncl = s->col_ncl;
+    a.overhang = s->overhang;
     a.rc = s->cutoff;
     a.rc2 = s->cutoff * s->cutoff;
     const double rs = s->rswitch > 0 ? s->rswitch : s->cutoff;

@@ -181,6 +181,19 @@ __global__ void k_col_scan(const int *__restrict__ col_ncl, int n_cols,
     if (threadIdx.x == 0) col_cl_start[n_cols] = carry;
 }
 
+// every cluster of a column learns its column (clusters past a column's
+// atoms, and past a system's used clusters, keep -1)
+__global__ void k_cluster_columns(const int *__restrict__ col_ncl,
+                                  const int *__restrict__ col_cl_start, int n_cols,
+                                  const SysDev *__restrict__ sys, const int *__restrict__ col_sys,
+                                  int *__restrict__ cl_col) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cols) return;
+    const SysDev &d = sys[col_sys[c]];
+    const int first = d.cl_off + col_cl_start[c] - col_cl_start[d.col_off];
+    for (int k = 0; k < col_ncl[c]; ++k) cl_col[first + k] = c;
+}
+
 // atom of global rank g goes to its column's cluster block, in rank order;
 // each system's clusters start at its fixed offset cl_off
 __global__ void k_finish_perm(const int *__restrict__ tmp, const int *__restrict__ key, int n,
@@ -247,7 +260,9 @@ __global__ void k_partners_sorted(const int *__restrict__ perm, const int *__res
 __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ perm,
                        const float *__restrict__ q_sorted, int n_clusters, int n_pad,
                        float4 *__restrict__ xq, float4 *__restrict__ bbox,
-                       unsigned long long *__restrict__ f) {
+                       unsigned long long *__restrict__ f, const SysDev *__restrict__ sys,
+                       const int *__restrict__ cl_sys, const int *__restrict__ cl_col,
+                       const int *__restrict__ col_xy, float *__restrict__ overhang) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (warp >= n_clusters) return;
@@ -256,7 +271,20 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ per
     float4 p;
     bool valid = i >= 0;
     if (valid) {
-        p = make_float4((float)x[3 * i], (float)x[3 * i + 1], (float)x[3 * i + 2], q_sorted[k]);
+        // Between re-sorts the FP64 positions drift freely out of [0, L).
+        // The pair search tries the images -1, 0, +1 of each cluster pair,
+        // which is exact while every stored coordinate stays within a window
+        // of width 1.5 L: a coordinate that leaves [-L/4, 5L/4) is wrapped
+        // back into [0, L) here (its cluster box then spans the box, and the
+        // search covers it with all 27 images).
+        const double *Ld = sys[cl_sys[warp]].Ld;
+        double c[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            c[d] = x[3 * i + d];
+            if (c[d] < -0.25 * Ld[d] || c[d] >= 1.25 * Ld[d]) c[d] -= Ld[d] * floor(c[d] / Ld[d]);
+        }
+        p = make_float4((float)c[0], (float)c[1], (float)c[2], q_sorted[k]);
     } else {
         p = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
     }
@@ -286,6 +314,20 @@ __global__ void k_pack(const double *__restrict__ x, const int *__restrict__ per
                                          0.5f * (loz + hiz), (float)cnt);
             bbox[2 * warp + 1] = make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy),
                                              0.5f * (hiz - loz), 0.0f);
+            // how far the box reaches out of its sort column in x and y
+            const int c = cl_col[warp];
+            if (c >= 0) {
+                const int q = cl_sys[warp];
+                const SysDev &d = sys[q];
+                const int pk = col_xy[c];
+                const float ax = d.L[0] / (float)d.ncx, ay = d.L[1] / (float)d.ncy;
+                const float x0 = (float)(pk >> 16) * ax, y0 = (float)(pk & 0xffff) * ay;
+                const float ov = fmaxf(fmaxf(fmaxf(x0 - lox, hix - (x0 + ax)),
+                                             fmaxf(y0 - loy, hiy - (y0 + ay))),
+                                       0.0f);
+                if (ov > overhang[q])
+                    atomicMax((unsigned int *)&overhang[q], __float_as_uint(ov));
+            }
         }
     }
 }
@@ -313,7 +355,7 @@ int realloc_dev(T **p, size_t count) {
 // and every buffer whose size depends on them (the cluster-order arrays are
 // sized for the worst-case padding: one partial cluster per column)
 int prepare_sort_grid(mdg_system *s) {
-    std::vector<int> col_rank_all, col_sys, cl_sys;
+    std::vector<int> col_rank_all, col_sys, cl_sys, col_xy;
     int col_off = 0, key_off = 0, cl_off = 0;
     for (int q = 0; q < s->n_sys; ++q) {
         SysDev &d = s->sys_h[q];
@@ -333,8 +375,16 @@ int prepare_sort_grid(mdg_system *s) {
             for (int cy = 0; cy < d.ncy; ++cy)
                 codes[cx * d.ncy + cy] = {spread2(cx) | (spread2(cy) << 1), cx * d.ncy + cy};
         std::sort(codes.begin(), codes.end());
-        std::vector<int> rank(d.n_cols);
-        for (int r = 0; r < d.n_cols; ++r) rank[codes[r].second] = r;
+        std::vector<int> rank(d.n_cols), xy(d.n_cols);
+        for (int r = 0; r < d.n_cols; ++r) {
+            const int cxy = codes[r].second;
+            rank[cxy] = r;
+            xy[r] = ((cxy / d.ncy) << 16) | (cxy % d.ncy);
+        }
+        // neighbour-column pair search needs at least 5 columns per axis
+        // (whether the reach fits is decided on the device every step)
+        d.col_mode = (d.ncx >= 5 && d.ncy >= 5) ? 1 : 0;
+        col_xy.insert(col_xy.end(), xy.begin(), xy.end());
         col_rank_all.insert(col_rank_all.end(), rank.begin(), rank.end());
         col_sys.insert(col_sys.end(), d.n_cols, q);
         cl_sys.insert(cl_sys.end(), d.cl_cap, q);
@@ -354,7 +404,8 @@ int prepare_sort_grid(mdg_system *s) {
         (rc = realloc_dev(&s->cell_cursor, key_off)) ||
         (rc = realloc_dev(&s->scan_blocks, s->n_scan_blocks)) ||
         (rc = realloc_dev(&s->col_ncl, col_off)) || (rc = realloc_dev(&s->col_cl_start, col_off + 1)) ||
-        (rc = realloc_dev(&s->col_sys, col_off)))
+        (rc = realloc_dev(&s->col_sys, col_off)) || (rc = realloc_dev(&s->col_xy, col_off)) ||
+        (rc = realloc_dev(&s->overhang, s->n_sys)))
         return rc;
     if (n_pad != s->n_pad || !s->perm) {
         s->n_pad = n_pad;
@@ -365,6 +416,7 @@ int prepare_sort_grid(mdg_system *s) {
             (rc = realloc_dev(&s->bbox, 2 * (size_t)n_clusters)) ||
             (rc = realloc_dev(&s->cluster_partner_range, n_clusters)) ||
             (rc = realloc_dev(&s->cl_sys, n_clusters)) ||
+            (rc = realloc_dev(&s->cl_col, n_clusters)) ||
             (rc = realloc_dev(&s->partners_sorted, (size_t)n_pad * std::max(s->pw, 1))))
             return rc;
         if (cudaMemset(s->f, 0, sizeof(unsigned long long) * 3 * n_pad) != cudaSuccess)
@@ -373,6 +425,8 @@ int prepare_sort_grid(mdg_system *s) {
     if (cudaMemcpy(s->cell_rank, col_rank_all.data(), sizeof(int) * col_off,
                    cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(s->col_sys, col_sys.data(), sizeof(int) * col_off, cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(s->col_xy, col_xy.data(), sizeof(int) * col_off, cudaMemcpyHostToDevice) !=
             cudaSuccess ||
         cudaMemcpy(s->cl_sys, cl_sys.data(), sizeof(int) * n_clusters, cudaMemcpyHostToDevice) !=
             cudaSuccess)
@@ -398,6 +452,8 @@ cudaError_t launch_reorder(mdg_system *s) {
     cudaMemsetAsync(s->perm, 0xff, sizeof(int) * s->n_pad, st);
     cudaMemsetAsync(s->q_sorted, 0, sizeof(float) * s->n_pad, st);
     cudaMemsetAsync(s->prm_sorted, 0, sizeof(float2) * s->n_pad, st);
+    cudaMemsetAsync(s->cl_col, 0xff, sizeof(int) * s->n_clusters, st);
+    cudaMemsetAsync(s->overhang, 0, sizeof(float) * s->n_sys, st);
     k_bin<<<(n + tb - 1) / tb, tb, 0, st>>>(s->x, n, s->sys_dev, s->atom_sys, s->cell_rank,
                                             s->atom_key, s->cell_count, s->status);
     k_block_sums<<<s->n_scan_blocks, kScanThreads, 0, st>>>(s->cell_count, s->n_cells,
@@ -408,6 +464,9 @@ cudaError_t launch_reorder(mdg_system *s) {
     k_col_clusters<<<(s->n_cols + tb - 1) / tb, tb, 0, st>>>(s->cell_start, s->n_cols,
                                                              s->sys_dev, s->col_sys, s->col_ncl);
     k_col_scan<<<1, kScanThreads, 0, st>>>(s->col_ncl, s->n_cols, s->col_cl_start);
+    k_cluster_columns<<<(s->n_cols + tb - 1) / tb, tb, 0, st>>>(s->col_ncl, s->col_cl_start,
+                                                                s->n_cols, s->sys_dev, s->col_sys,
+                                                                s->cl_col);
     k_scatter<<<(n + tb - 1) / tb, tb, 0, st>>>(s->atom_key, n, s->cell_start, s->cell_cursor,
                                                 s->tmp_perm);
     k_cell_sort<<<(s->n_cells + tb - 1) / tb, tb, 0, st>>>(s->cell_start, s->n_cells, s->tmp_perm);
@@ -419,14 +478,15 @@ cudaError_t launch_reorder(mdg_system *s) {
     k_partners_sorted<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, st>>>(
         s->perm, s->inv_perm, s->partners, s->pw, s->n_clusters, s->partners_sorted,
         s->cluster_partner_range);
-    s->launches += 10;
+    s->launches += 11;
     return cudaGetLastError();
 }
 
 cudaError_t launch_pack(mdg_system *s) {
     const int tb = 256;
     k_pack<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, s->stream>>>(
-        s->x, s->perm, s->q_sorted, s->n_clusters, s->n_pad, s->xq, s->bbox, s->f);
+        s->x, s->perm, s->q_sorted, s->n_clusters, s->n_pad, s->xq, s->bbox, s->f, s->sys_dev,
+        s->cl_sys, s->cl_col, s->col_xy, s->overhang);
     s->launches += 1;
     return cudaGetLastError();
 }

@@ -99,8 +99,18 @@ class Simulation:
     def reset_simulation_step(self):
         self._cur_step = 0
 
+    def set_minimizer(self, minimizer):
+        self._minimizer = minimizer
+
     def minimize(self, energy_tolerance, max_iterations):
-        raise NotImplementedError("energy minimisation is not part of the device hot path")
+        """mdpy/simulation.py:52-54; the default minimizer is steepest descent
+        with alpha 0.01 A (:18)."""
+        if self._minimizer is None:
+            from .minimizer import SteepestDescentMinimizer
+
+            self._minimizer = SteepestDescentMinimizer(0.01)
+        self._minimizer.minimize(self._ensemble, energy_tolerance, max_iterations)
+        self._dump()
 
     def integrate(self, num_steps: int):
         if not self._dumpers or self._minimum_dump_frequency == 0:

@@ -1,0 +1,84 @@
+"""Pair search over neighbouring sort columns (large boxes): the pair set is
+the brute-force set at every reach the search uses (R = 2, R = 3, and the
+full-scan fallback when 2R+1 columns no longer fit), also after the atoms
+have drifted far from their sort columns without a re-sort; forces match the
+FP64 oracle."""
+import numpy as np
+import pytest
+
+from tests.helpers import make_system, min_image_r, pairs_to_set, rel_rms, water_lj_rows
+
+EPS_BAND = 1e-4  # A: pairs this close to rc may fall either side in FP32
+
+
+def _same_pairs(gpu, bf, pos, box, rc):
+    """Equal sets up to pairs within EPS_BAND of the cutoff."""
+    diff = sorted(gpu ^ bf)
+    if diff:
+        r = min_image_r(pos, box, diff)
+        assert np.all(np.abs(r - rc) <= EPS_BAND), [(p, x) for p, x in zip(diff, r)][:5]
+    assert len(diff) <= 1e-5 * len(bf) + 5
+
+pytestmark = pytest.mark.gpu
+
+
+def _box():
+    from mdpy_gb300 import systems
+
+    return systems.water_box(5000, 53.0, seed=21)   # 15,000 atoms, 8 x 8 columns
+
+
+@pytest.mark.parametrize("rc", [10.0, 14.0, 20.0])
+def test_column_pair_set_equals_bruteforce(lib, orc, rc):
+    w = _box()
+    n = w.num_particles
+    none = np.full((n, 1), -1)
+    s = make_system(lib, n, w.box, lj=water_lj_rows(w), charges=np.zeros(n), bonded=none,
+                    cutoff=rc, positions=w.positions)
+    gpu = pairs_to_set(s.pairset())
+    bf = pairs_to_set(orc.pairs_bruteforce(w.positions, w.box, rc))
+    _same_pairs(gpu, bf, w.positions, w.box, rc)
+    s.compute_forces(lib.mask(lib.TERM_LJ))
+    assert s.nonbonded_stats()["pairs_in_cutoff"] == len(gpu)
+
+
+@pytest.mark.parametrize("n_waters,edge", [(5000, 53.0), (900, 30.0)])
+def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge):
+    """400 Langevin steps at 900 K with no re-sort: unbonded H atoms fly
+    tens of A, past the periodic box; the pair set still equals brute force
+    (53 A: neighbour-column search; 30 A: full scan with 27 images)."""
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(n_waters, edge, seed=21)
+    n = w.num_particles
+    none = np.full((n, 1), -1)
+    s = make_system(lib, n, w.box, masses=w.topology.masses.reshape(-1), lj=water_lj_rows(w),
+                    charges=np.zeros(n), bonded=none, cutoff=12.0, positions=w.positions,
+                    velocities=systems.maxwell_boltzmann(np.random.default_rng(3),
+                                                         w.topology.masses, 900.0))
+    s.set_reorder_interval(100000)
+    s.integrator_config(lib.INTEGRATOR_LANGEVIN, 1.0, 900.0, 0.001, 7)
+    s.integrate(400, lib.mask(lib.TERM_LJ), want_energy=False)
+    x = s.get_positions()
+    gpu = pairs_to_set(s.pairset())
+    bf = pairs_to_set(orc.pairs_bruteforce(x, w.box, 12.0))
+    _same_pairs(gpu, bf, x, w.box, 12.0)
+
+
+def test_column_forces_vs_oracle(lib, orc):
+    w = _box()
+    t = w.topology
+    n = w.num_particles
+    beta = orc.ewald_beta(12.0, 1e-5)
+    lj = water_lj_rows(w)
+    s = make_system(lib, n, w.box, charges=t.charges.reshape(-1), lj=lj,
+                    bonded=t.bonded_particles, scaling=t.scaling_particles, cutoff=12.0,
+                    switch=10.0, coulomb=lib.COUL_EWALD, beta=beta, positions=w.positions)
+    s.compute_forces(lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL))
+    f = s.get_forces()
+    e, _ = s.get_energies()
+    fo, eo = orc.nonbonded(w.positions, w.box, lj, t.charges, t.bonded_particles,
+                           t.scaling_particles, 12.0, switch=10.0, coulomb="ewald", beta=beta)
+    assert rel_rms(f, fo) <= 1e-5
+    assert e[lib.TERM_LJ] == pytest.approx(eo["lj"], rel=1e-5)
+    assert e[lib.TERM_COUL_REAL] == pytest.approx(eo["coulomb"], rel=1e-5)
