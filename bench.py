@@ -55,6 +55,8 @@ def parse():
                         "waters (1M atoms) in a 215 A box; batch256: 256 independent water "
                         "boxes of 1.5k-12k atoms in one batch")
     p.add_argument("--boxes", type=int, default=256)
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default launch shape instead of timing the alternatives")
     p.add_argument("--waters", type=int, default=None)
     p.add_argument("--box", type=float, default=None)
     p.add_argument("--beads", type=int, default=None)
@@ -175,6 +177,7 @@ def run_batch(a, world, rank, local):
     mask = b.term_mask
     sysm.set_graph_mode(_lib.GRAPH_STEP)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    shape = sysm.launch_shape if a.no_autotune else sysm.autotune(mask, reps=5)
     sysm.integrate(max(a.warmup, 3), mask, want_energy=False)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
@@ -234,7 +237,8 @@ def run_batch(a, world, rank, local):
                                    % (a.boxes, BATCH_CUTOFF, grids[0], grids[-1]),
                        "atoms": n, "boxes": a.boxes, "atoms_min": min(sizes),
                        "atoms_max": max(sizes), "pme_grids": grids,
-                       "l2": "flushed between timed steps (256 MB rewrite)", "form": "batched"},
+                       "l2": "flushed between timed steps (256 MB rewrite)", "form": "batched",
+                       "launch_shape": shape},
             "ns_per_day_per_box": ns_day_per_box,
             "one_at_a_time": {"ms_per_step_all_boxes": one_at_a_time_ms,
                               "atom_steps_per_s": n / (one_at_a_time_ms / 1000.0),
@@ -515,6 +519,7 @@ def main():
     mask = ens.term_mask
     sysm.set_graph_mode(_lib.GRAPH_STEP)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    shape = sysm.launch_shape if a.no_autotune else sysm.autotune(mask, reps=10)
 
     # warm-up (graphs captured here)
     sysm.integrate(max(a.warmup, 3), mask, want_energy=False)
@@ -609,13 +614,11 @@ def main():
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
+    e_terms = np.zeros(_lib.NUM_TERMS)
     for k in range(a.e2e_steps):
-        sysm.set_positions_ptr(x_h.data_ptr(), _lib.HOST)
-        sysm.set_velocities_ptr(v_h.data_ptr(), _lib.HOST)
-        sysm.integrate(1, mask, want_energy=True)
-        sysm.get_positions_ptr(x_h.data_ptr(), _lib.HOST)
-        sysm.get_velocities_ptr(v_h.data_ptr(), _lib.HOST)
-        e_terms, ke = sysm.get_energies()
+        # one C-ABI call: host state in, one step, host state and energies out
+        sysm.step_host_ptr(x_h.data_ptr(), v_h.data_ptr(), 1, mask, x_h.data_ptr(),
+                           v_h.data_ptr(), e_terms)
     torch.cuda.synchronize()
     e2e_s = reduce_max(time.perf_counter() - t0, world,
                        device=torch.device("cuda", local)
@@ -624,8 +627,23 @@ def main():
     e2e_value = unit.ns_per_day(world * a.e2e_steps / e2e_s, DT_FS)
     e2e = {"value": e2e_value, "unit": "ns/day", "h2d_bytes_per_step": 2 * n * 24,
            "d2h_bytes_per_step": 2 * n * 24 + 8 * (_lib.NUM_TERMS + 1),
-           "api": "mdg_set_positions/velocities(host) + mdg_integrate(1) + "
-                  "mdg_get_positions/velocities(host) + mdg_get_energies"}
+           "api": "mdg_step_host: positions + velocities in from pinned host memory, one "
+                  "step (starting with a re-sort, as new host positions require), wrapped "
+                  "positions + velocities + energies out, one synchronisation"}
+
+    # what a multiple-time-step scheme could save at most: the same step
+    # with the reciprocal-space term left out (PME runs beside the pair
+    # kernel on the side stream, so only its share of the SMs shows)
+    from mdpy_gb300 import _lib as L_
+
+    no_pme = mask & ~L_.mask(L_.TERM_COUL_RECIP)
+    sysm.integrate(5, no_pme, want_energy=False)
+    reps = max(50, a.steps // 4)
+    ms_no_pme = time_steps(sysm, no_pme, reps, stream, flush) / reps
+    sysm.integrate(5, mask, want_energy=False)
+    mts_bound = {"ms_per_step_without_pme": ms_no_pme, "ms_per_step": ms_step,
+                 "pme_share_of_step": 1.0 - ms_no_pme / ms_step,
+                 "max_saving_pme_every_4_steps": 0.75 * (1.0 - ms_no_pme / ms_step)}
 
     nve = nve_drift(sysm, mask, n, a.nve_ps) if a.nve_ps > 0 else None
 
@@ -651,10 +669,11 @@ def main():
                        "l2": "flushed between timed steps (256 MB rewrite)",
                        "precision": "f32 pair/PME arithmetic, int64 fixed-point (2^-32) force "
                                     "accumulation, f64 x/v/energies",
-                       "form": "plain"},
+                       "form": "plain", "launch_shape": shape},
             "atom_steps_per_s": n * sps_job,
             "force_rel_rms_err_vs_fp64": err,
             "nve_drift": nve,
+            "mts_bound": mts_bound,
             "plain": plain, "chosen": dict(plain, form="plain"),
             "roofline": roofline, "stages_ms": stage_ms, "nonbonded_stats": stats,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),

@@ -168,6 +168,59 @@ MDG_API int mdg_get_energies(mdg_system *sys, double *energies, double *kinetic)
 /* Ensemble._update_kinetic_energy (mdpy/ensemble.py:63-71), FP64 */
 MDG_API int mdg_kinetic_energy(mdg_system *sys, double *kinetic);
 
+/* One call for a host-driven loop (no reference counterpart; it bundles
+ * State.set_positions/set_velocities, Integrator.integrate and the reads of
+ * State.positions/velocities and the energies): copies x_in / v_in (host,
+ * (n,3); NULL = keep the device state) to the device, runs n_steps steps of
+ * the configured integrator on the terms in `mask`, copies the wrapped
+ * positions, the velocities (host (n,3); NULL = skip) and the energies
+ * (energies[MDG_NUM_TERMS], *kinetic; NULL = skip) back, all on the system's
+ * stream with one synchronisation at the end.  New positions start with a
+ * re-sort, as mdg_set_positions does. */
+MDG_API int mdg_step_host(mdg_system *sys, const double *x_in, const double *v_in, int n_steps,
+                          unsigned mask, double *x_out, double *v_out, double *energies,
+                          double *kinetic);
+
+/* ---- launch shapes and the autotuner (no reference counterpart) ---------
+ * A launch shape is MDG_SHAPE_FIELDS ints:
+ *   [MDG_SHAPE_SPLIT]          work items (one warp each) per 32-atom cluster in
+ *                              the pair kernel: 1, 2, 4, 8, 16 (default 4);
+ *   [MDG_SHAPE_PERSISTENT]     0 = one CTA per work item; n = n resident CTAs
+ *                              per SM (1..24) pulling work items from a device
+ *                              counter (default 0);
+ *   [MDG_SHAPE_PME_BLOCK]      threads per block of PME spread/gather: 64, 128,
+ *                              256 (default 256);
+ *   [MDG_SHAPE_SIDE_PRIORITY]  1 runs PME, special pairs and bonded terms on
+ *                              highest-priority streams beside the pair kernel
+ *                              (default 0);
+ *   [MDG_SHAPE_SPLIT_RINGS]    1 sweeps j atoms without LJ parameters in chunks
+ *                              that skip the LJ arithmetic (default 1);
+ *   [MDG_SHAPE_PME_TILES]      bit 0: spreading through a shared-memory tile of
+ *                              the block's grid patch, bit 1: gathering from one
+ *                              (default 0).
+ * Results depend on the shape only through float rounding of partial sums
+ * (the PME grid and tiling change nothing: int64 sums); for a fixed shape
+ * they are bit-reproducible. */
+#define MDG_SHAPE_SPLIT 0
+#define MDG_SHAPE_PERSISTENT 1
+#define MDG_SHAPE_PME_BLOCK 2
+#define MDG_SHAPE_SIDE_PRIORITY 3
+#define MDG_SHAPE_SPLIT_RINGS 4
+#define MDG_SHAPE_PME_TILES 5
+#define MDG_SHAPE_FIELDS 6
+MDG_API int mdg_set_launch_shape(mdg_system *sys, const int *shape);
+MDG_API int mdg_get_launch_shape(mdg_system *sys, int *shape);
+/* Picks the fastest launch shape: with an integrator configured it times MD
+ * steps as mdg_integrate runs them (captured single-step graphs replayed from
+ * a saved state, which is restored afterwards), else force evaluations of
+ * `mask`.  Phase one varies the pair kernel (split 2/4/8 x persistent 0/20/24
+ * x split rings 0/1), phase two PME and the streams (block 64/128/256 x tiles
+ * 0-3 x side priority 0/1) around phase one's best; then the four fastest and
+ * the shape in use are re-timed, interleaved, over 4 x reps and the fastest
+ * is kept; *best_ms (may be NULL) receives its time.  Leaves no valid force
+ * evaluation. */
+MDG_API int mdg_autotune(mdg_system *sys, unsigned mask, int reps, double *best_ms);
+
 /* ---- energy minimisation ------------------------------------------------ */
 /* One move of SteepestDescentMinimizer.minimize
  * (mdpy/minimizer/steepest_descent_minimizer.py:39-42): x_i += alpha F_i/|F_i|

@@ -76,6 +76,11 @@ SIGNATURES = {
     "mdg_kinetic_energy": [_sys_p, _c_dbl_p],
     "mdg_kinetic_energies_noalloc": [_sys_p, _c_dbl_p],
     "mdg_minimize_step": [_sys_p, ctypes.c_double],
+    "mdg_step_host": [_sys_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint,
+                      ctypes.c_void_p, ctypes.c_void_p, _c_dbl_p, _c_dbl_p],
+    "mdg_set_launch_shape": [_sys_p, _c_int_p],
+    "mdg_get_launch_shape": [_sys_p, _c_int_p],
+    "mdg_autotune": [_sys_p, ctypes.c_uint, ctypes.c_int, _c_dbl_p],
     "mdg_integrator_config": [_sys_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                               ctypes.c_double, ctypes.c_uint64],
     "mdg_integrate": [_sys_p, ctypes.c_int, ctypes.c_uint, ctypes.c_int],
@@ -308,6 +313,44 @@ class System:
         ke = ctypes.c_double(0.0)
         check(self._lib.mdg_get_energies(self._h, _dp(e), ctypes.byref(ke)))
         return e, ke.value
+
+    SHAPE_FIELDS = ("split", "persistent", "pme_block", "side_priority", "split_rings",
+                    "pme_tiles")
+
+    def set_launch_shape(self, split=4, persistent=0, pme_block=256, side_priority=0,
+                         split_rings=1, pme_tiles=0):
+        """``persistent``: 0 = one CTA per pair work item, n = n resident CTAs
+        per SM pulling work items; ``pme_tiles``: bit 0 tiled spreading, bit 1
+        tiled gathering."""
+        sh = (ctypes.c_int * 6)(int(split), int(persistent), int(pme_block), int(side_priority),
+                                int(split_rings), int(pme_tiles))
+        check(self._lib.mdg_set_launch_shape(self._h, sh))
+
+    @property
+    def launch_shape(self):
+        sh = (ctypes.c_int * 6)()
+        check(self._lib.mdg_get_launch_shape(self._h, sh))
+        return dict(zip(self.SHAPE_FIELDS, list(sh)))
+
+    def autotune(self, term_mask=MASK_ALL, reps=10):
+        """Pick the fastest launch shape (MD steps when an integrator is
+        configured, force evaluations otherwise); returns the shape and its
+        time (ms per step or evaluation)."""
+        best = ctypes.c_double(0.0)
+        check(self._lib.mdg_autotune(self._h, int(term_mask), int(reps), ctypes.byref(best)))
+        return dict(self.launch_shape, tuned_ms=best.value)
+
+    def step_host_ptr(self, x_in, v_in, n_steps, term_mask, x_out, v_out, energies=None,
+                      want_kinetic=True):
+        """mdg_step_host with raw host addresses (0 = skip); ``energies``: a
+        float64 array of NUM_TERMS or None.  Returns the kinetic energy."""
+        ke = ctypes.c_double(0.0)
+        check(self._lib.mdg_step_host(
+            self._h, ctypes.c_void_p(x_in or None), ctypes.c_void_p(v_in or None), int(n_steps),
+            int(term_mask), ctypes.c_void_p(x_out or None), ctypes.c_void_p(v_out or None),
+            None if energies is None else _dp(energies),
+            ctypes.byref(ke) if want_kinetic else None))
+        return ke.value
 
     def minimize_step(self, alpha):
         check(self._lib.mdg_minimize_step(self._h, float(alpha)))

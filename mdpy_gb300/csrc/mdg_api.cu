@@ -78,8 +78,9 @@ void drop_one(Graph &g) {
 
 void drop_graph(mdg_system *s) {
     drop_one(s->graph);
-    drop_one(s->graph_step[0]);
-    drop_one(s->graph_step[1]);
+    for (auto &row : s->graph_step)
+        for (Graph &g : row) drop_one(g);
+    for (Graph &g : s->graph_eval) drop_one(g);
 }
 
 int validate_box(const double *box, double cutoff) {
@@ -131,11 +132,7 @@ void ewald_constants(mdg_system *s) {
     }
 }
 
-int read_status(mdg_system *s) {
-    int st = 0;
-    CK(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
-       "status read");
-    CK(cudaStreamSynchronize(s->stream), "synchronize");
+int decode_status(mdg_system *s, int st) {
     if (st) {
         CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
         for (int code = 1; code < 31; ++code)
@@ -153,6 +150,14 @@ int read_status(mdg_system *s) {
     return MDG_OK;
 }
 
+int read_status(mdg_system *s) {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+       "status read");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return decode_status(s, st);
+}
+
 int evaluate(mdg_system *s, unsigned mask, int energy) {
     if (s->need_reorder) {
         CK(launch_reorder(s), "reorder");
@@ -165,29 +170,35 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
         CK(cudaMemsetAsync(s->stats, 0, sizeof(unsigned long long) * 4, s->stream), "memset");
     }
     CK(launch_pack(s), "pack");
-    // fork: PME, special pairs and bonded terms run on the side stream while
-    // the pair kernel runs on the main stream (all accumulate through
-    // order-independent fixed-point atomics); join before anything reads f
+    // fork: PME on one side stream, special pairs and bonded terms on
+    // another, while the pair kernel runs on the main stream (all accumulate
+    // through order-independent fixed-point atomics); join both before
+    // anything reads f
     CK(cudaEventRecord(s->ev_fork, s->stream), "fork");
     CK(cudaStreamWaitEvent(s->side_stream, s->ev_fork, 0), "fork wait");
+    CK(cudaStreamWaitEvent(s->bond_stream, s->ev_fork, 0), "fork wait");
     cudaStream_t main = s->stream;
-    s->stream = s->side_stream;
     int rc = MDG_OK;
     cudaError_t e = cudaSuccess;
+    s->stream = s->side_stream;
     if ((mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on) {
         int cr = 0;
         e = launch_pme(s, energy, &cr);
         if (cr != CUFFT_SUCCESS) rc = fail(MDG_ERR_CUFFT, "cuFFT execution failed (%d)", cr);
     }
+    cudaError_t ej = cudaEventRecord(s->ev_join, s->side_stream);
+    s->stream = s->bond_stream;
     if (!rc && e == cudaSuccess) e = launch_special(s, mask, energy, 0);
     if (!rc && e == cudaSuccess) e = launch_bonded(s, mask, energy);
-    cudaError_t ej = cudaEventRecord(s->ev_join, s->side_stream);
+    cudaError_t ej2 = cudaEventRecord(s->ev_join2, s->bond_stream);
     s->stream = main;
     if (rc) return rc;
     CK(e, "side-stream terms");
     CK(ej, "join");
+    CK(ej2, "join");
     CK(launch_nonbonded(s, mask, energy, 0), "nonbonded");
     CK(cudaStreamWaitEvent(s->stream, s->ev_join, 0), "join wait");
+    CK(cudaStreamWaitEvent(s->stream, s->ev_join2, 0), "join wait");
     s->evaluated_once = 1;
     return MDG_OK;
 }
@@ -206,7 +217,8 @@ int md_step(mdg_system *s, unsigned mask, int energy) {
 // Capture `nsteps` MD steps (the first re-sorting the atoms when `resort`)
 // into g; host-side counters are restored, the launch count per replay is
 // kept in g.steps.
-int capture_steps(mdg_system *s, Graph &g, int nsteps, int resort, unsigned mask) {
+int capture_steps(mdg_system *s, Graph &g, int nsteps, int resort, unsigned mask,
+                  int energy_last = 0) {
     const long long saved = s->launches;
     const int saved_since = s->steps_since_reorder, saved_need = s->need_reorder;
     const uint64_t saved_step = s->step;
@@ -214,12 +226,43 @@ int capture_steps(mdg_system *s, Graph &g, int nsteps, int resort, unsigned mask
     if (!resort) s->steps_since_reorder = 0;
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture");
     int crc = MDG_OK;
-    for (int k = 0; k < nsteps && !crc; ++k) crc = md_step(s, mask, 0);
+    for (int k = 0; k < nsteps && !crc; ++k)
+        crc = md_step(s, mask, (energy_last && k == nsteps - 1) ? 1 : 0);
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
     s->steps_since_reorder = saved_since;
     s->need_reorder = saved_need;
     s->step = saved_step;
+    const long long per = s->launches - saved;
+    s->launches = saved;
+    if (crc) {
+        if (graph) cudaGraphDestroy(graph);
+        return crc;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "end capture");
+    ce = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+        g.exec = nullptr;
+        return cuda_fail(ce, "graph instantiate");
+    }
+    g.steps = (int)per;
+    g.mask = mask;
+    return MDG_OK;
+}
+
+// The force evaluation an integration starts with when the forces are not
+// valid (new positions): captured once per re-sort flag and replayed.
+int capture_eval(mdg_system *s, Graph &g, int resort, unsigned mask) {
+    const long long saved = s->launches;
+    const int saved_need = s->need_reorder, saved_since = s->steps_since_reorder;
+    s->need_reorder = resort ? 1 : 0;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture");
+    const int crc = evaluate(s, mask, 0);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
+    s->need_reorder = saved_need;
+    s->steps_since_reorder = saved_since;
     const long long per = s->launches - saved;
     s->launches = saved;
     if (crc) {
@@ -309,9 +352,25 @@ MDG_API int mdg_system_create_batch(int device, int n_systems, const int *n_atom
         return cuda_fail(e, "cudaStreamCreate");
     }
     s->stream = s->own_stream;
-    e = cudaStreamCreateWithFlags(&s->side_stream, cudaStreamNonBlocking);
+    {
+        // two side streams: normal priority, and the highest priority (its
+        // small kernels then take free SM slots ahead of the pair kernel's
+        // queued CTAs); the launch shape picks one
+        int lo = 0, hi = 0;
+        e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+            e = cudaStreamCreateWithPriority(&s->side_streams[k], cudaStreamNonBlocking,
+                                             k ? hi : lo);
+            if (e == cudaSuccess)
+                e = cudaStreamCreateWithPriority(&s->bond_streams[k], cudaStreamNonBlocking,
+                                                 k ? hi : lo);
+        }
+        s->side_stream = s->side_streams[0];
+        s->bond_stream = s->bond_streams[0];
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join2, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         mdg_system_destroy(s);
         return cuda_fail(e, "side stream");
@@ -340,7 +399,13 @@ MDG_API int mdg_system_create_batch(int device, int n_systems, const int *n_atom
     AL(s->fout, 3 * (size_t)n);
     AL(s->dump_count, 1);
     AL(s->partners, 1);
+    AL(s->nb_queue, 1);
 #undef AL
+    {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        s->n_sms = std::max(1, sms);
+    }
     cudaMemset(s->energy, 0, sizeof(long long) * kEnergySlots * n_systems);
     cudaMemset(s->status, 0, sizeof(int));
     cudaMemset(s->step_dev, 0, sizeof(unsigned long long));
@@ -402,6 +467,7 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->cl_sys);
     dfree(s->col_sys);
     dfree(s->cl_col);
+    dfree(s->nb_queue);
     dfree(s->col_xy);
     dfree(s->overhang);
     dfree(s->sys_dev);
@@ -427,13 +493,17 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->dih_prm);
     dfree(s->imp_idx);
     dfree(s->imp_prm);
-    if (s->side_stream) {
-        cudaStreamSynchronize(s->side_stream);
-        cudaStreamDestroy(s->side_stream);
-    }
+    for (cudaStream_t *pair : {s->side_streams, s->bond_streams})
+        for (int k = 0; k < 2; ++k)
+            if (pair[k]) {
+                cudaStreamSynchronize(pair[k]);
+                cudaStreamDestroy(pair[k]);
+            }
+    if (s->ev_join2) cudaEventDestroy(s->ev_join2);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    if (s->host_stage) cudaFreeHost(s->host_stage);
     delete s;
     return MDG_OK;
 }
@@ -948,6 +1018,206 @@ MDG_API int mdg_kinetic_energies_noalloc(mdg_system *s, double *kinetic) {
     return MDG_OK;
 }
 
+static int apply_shape(mdg_system *s, const int *sh) {
+    const int split = sh[MDG_SHAPE_SPLIT], persistent = sh[MDG_SHAPE_PERSISTENT],
+              pme_block = sh[MDG_SHAPE_PME_BLOCK], side_priority = sh[MDG_SHAPE_SIDE_PRIORITY],
+              split_rings = sh[MDG_SHAPE_SPLIT_RINGS], pme_tiles = sh[MDG_SHAPE_PME_TILES];
+    if (split != 1 && split != 2 && split != 4 && split != 8 && split != 16)
+        return fail(MDG_ERR_INVALID, "split %d is not 1, 2, 4, 8 or 16", split);
+    if (persistent < 0 || persistent > 24)
+        return fail(MDG_ERR_INVALID, "persistent CTAs per SM %d not in 0..24", persistent);
+    if (pme_block != 64 && pme_block != 128 && pme_block != 256)
+        return fail(MDG_ERR_INVALID, "PME block %d is not 64, 128 or 256", pme_block);
+    if (side_priority != 0 && side_priority != 1)
+        return fail(MDG_ERR_INVALID, "side priority must be 0 or 1");
+    if (split_rings != 0 && split_rings != 1)
+        return fail(MDG_ERR_INVALID, "split_rings must be 0 or 1");
+    if (pme_tiles < 0 || pme_tiles > 3)
+        return fail(MDG_ERR_INVALID, "pme_tiles %d not in 0..3", pme_tiles);
+    s->nb_split = split;
+    s->nb_persistent = persistent;
+    s->nb_persistent_ctas = persistent * s->n_sms;
+    s->pme_block = pme_block;
+    s->side_priority = side_priority;
+    s->side_stream = s->side_streams[side_priority];
+    s->bond_stream = s->bond_streams[side_priority];
+    s->nb_split_rings = split_rings;
+    s->pme_tiles = pme_tiles;
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+static void current_shape(const mdg_system *s, int *sh) {
+    sh[MDG_SHAPE_SPLIT] = s->nb_split;
+    sh[MDG_SHAPE_PERSISTENT] = s->nb_persistent;
+    sh[MDG_SHAPE_PME_BLOCK] = s->pme_block;
+    sh[MDG_SHAPE_SIDE_PRIORITY] = s->side_priority;
+    sh[MDG_SHAPE_SPLIT_RINGS] = s->nb_split_rings;
+    sh[MDG_SHAPE_PME_TILES] = s->pme_tiles;
+}
+
+MDG_API int mdg_set_launch_shape(mdg_system *s, const int *shape) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!shape) return fail(MDG_ERR_INVALID, "shape is null");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    CK(cudaStreamSynchronize(s->side_stream), "synchronize");
+    CK(cudaStreamSynchronize(s->bond_stream), "synchronize");
+    return apply_shape(s, shape);
+}
+
+MDG_API int mdg_get_launch_shape(mdg_system *s, int *shape) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!shape) return fail(MDG_ERR_INVALID, "shape is null");
+    current_shape(s, shape);
+    return MDG_OK;
+}
+
+// The autotuner.  With an integrator configured it times MD steps exactly
+// as mdg_integrate runs them (one captured single-step graph per shape,
+// replayed from the saved state, each replay between its own pair of events
+// so host launch gaps do not count), and puts the state back afterwards;
+// otherwise it times force evaluations of `mask`.  Phase one varies the pair
+// kernel (work items per cluster 2/4/8 x one CTA per item or 20/24 resident
+// CTAs per SM x split rings) with the PME fields of the shape in use; phase
+// two varies PME and the streams (block 64/128/256 x tiles 0-3 x side
+// priority) with phase one's best pair kernel; phase three re-times the four
+// fastest and the shape in use, interleaved, 4 x reps each, and keeps the
+// fastest (shapes a percent apart are otherwise decided by noise).
+MDG_API int mdg_autotune(mdg_system *s, unsigned mask, int reps, double *best_ms) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    mask &= MDG_MASK_ALL;
+    rc = ready_for_forces(s, mask);
+    if (rc) return rc;
+    if (reps < 1 || reps > 1000) return fail(MDG_ERR_INVALID, "reps %d out of range", reps);
+    const bool steps = s->integ_kind >= 0 && s->have_masses;
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    rc = evaluate(s, mask, 0);  // re-sorted clusters, fresh boxes, valid forces
+    if (rc) return rc;
+    double *xs = nullptr, *vs = nullptr;
+    unsigned long long step_saved = 0;
+    if (steps) {
+        if ((rc = dalloc(&xs, 3 * (size_t)s->n)) || (rc = dalloc(&vs, 3 * (size_t)s->n))) {
+            dfree(xs);
+            return rc;
+        }
+        cudaMemcpyAsync(xs, s->x, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(vs, s->v, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(&step_saved, s->step_dev, sizeof(step_saved), cudaMemcpyDeviceToHost,
+                        s->stream);
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    struct Shape {
+        int sh[MDG_SHAPE_FIELDS];
+        float ms;
+    };
+    auto time_shape = [&](Shape &c, int n) -> int {
+        int r = apply_shape(s, c.sh);
+        Graph g;
+        if (!r && steps) {
+            cudaMemcpyAsync(s->x, xs, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
+                            s->stream);
+            cudaMemcpyAsync(s->v, vs, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
+                            s->stream);
+            r = evaluate(s, mask, 0);  // forces of the restored positions
+            if (!r) r = capture_steps(s, g, 1, 0, mask);
+        }
+        float total = 0.f;
+        for (int w = 0; w < 2 + n && !r && ce == cudaSuccess; ++w) {
+            ce = cudaEventRecord(e0, s->stream);
+            if (ce != cudaSuccess) break;
+            if (steps) ce = cudaGraphLaunch(g.exec, s->stream);
+            else r = evaluate(s, mask, 0);
+            if (r || ce != cudaSuccess) break;
+            ce = cudaEventRecord(e1, s->stream);
+            if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+            if (w >= 2) total += ms;
+        }
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        c.ms = total / n;
+        return r;
+    };
+    auto by_time = [](const Shape &x, const Shape &y) { return x.ms < y.ms; };
+    Shape current;
+    current_shape(s, current.sh);
+    current.ms = 0.f;
+    const bool pme = (mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on;
+    std::vector<Shape> tried;
+    // phase one: the pair kernel
+    for (int sp : {2, 4, 8})
+        for (int pe : {0, 20, 24})
+            for (int sr = 0; sr <= 1 && !rc && ce == cudaSuccess; ++sr) {
+                Shape c = current;
+                c.sh[MDG_SHAPE_SPLIT] = sp;
+                c.sh[MDG_SHAPE_PERSISTENT] = pe;
+                c.sh[MDG_SHAPE_SPLIT_RINGS] = sr;
+                rc = time_shape(c, reps);
+                tried.push_back(c);
+            }
+    // phase two: PME and the side streams
+    if (!rc && ce == cudaSuccess) {
+        const Shape base = *std::min_element(tried.begin(), tried.end(), by_time);
+        for (int bl : {64, 128, 256})
+            for (int tl = 0; tl < 4; ++tl)
+                for (int pr = 0; pr <= 1 && !rc && ce == cudaSuccess; ++pr) {
+                    if (!pme && (bl != 256 || tl != 0)) continue;
+                    Shape c = base;
+                    c.sh[MDG_SHAPE_PME_BLOCK] = bl;
+                    c.sh[MDG_SHAPE_PME_TILES] = tl;
+                    c.sh[MDG_SHAPE_SIDE_PRIORITY] = pr;
+                    rc = time_shape(c, reps);
+                    tried.push_back(c);
+                }
+    }
+    Shape best = current;
+    float best_t = 0.f;
+    if (!rc && ce == cudaSuccess) {
+        std::sort(tried.begin(), tried.end(), by_time);
+        std::vector<Shape> top(tried.begin(), tried.begin() + std::min<size_t>(4, tried.size()));
+        top.push_back(current);
+        std::vector<float> sum(top.size(), 0.f);
+        for (int round = 0; round < 4 && !rc && ce == cudaSuccess; ++round)
+            for (size_t k = 0; k < top.size() && !rc && ce == cudaSuccess; ++k) {
+                rc = time_shape(top[k], reps);
+                sum[k] += top[k].ms;
+            }
+        size_t b = 0;
+        for (size_t k = 1; k < top.size(); ++k)
+            if (sum[k] < sum[b]) b = k;
+        best = top[b];
+        best_t = sum[b] / 4.0f;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    const int ra = apply_shape(s, best.sh);
+    if (steps) {
+        // put the state back: positions, velocities, the noise counter
+        cudaMemcpyAsync(s->x, xs, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->v, vs, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice, s->stream);
+        cudaMemcpyAsync(s->step_dev, &step_saved, sizeof(step_saved), cudaMemcpyHostToDevice,
+                        s->stream);
+        cudaStreamSynchronize(s->stream);
+        dfree(xs);
+        dfree(vs);
+        s->need_reorder = 1;
+    }
+    s->forces_valid = 0;
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "autotune");
+    if (ra) return ra;
+    rc = read_status(s);
+    if (rc) return rc;
+    if (best_ms) *best_ms = best_t;
+    return MDG_OK;
+}
+
 MDG_API int mdg_minimize_step(mdg_system *s, double alpha) {
     int rc = check_sys(s);
     if (rc) return rc;
@@ -957,6 +1227,80 @@ MDG_API int mdg_minimize_step(mdg_system *s, double alpha) {
     CK(launch_sd_step(s, alpha), "steepest-descent step");
     s->forces_valid = 0;
     if (++s->steps_since_reorder >= s->reorder_interval) s->need_reorder = 1;
+    return MDG_OK;
+}
+
+MDG_API int mdg_step_host(mdg_system *s, const double *x_in, const double *v_in, int n_steps,
+                          unsigned mask, double *x_out, double *v_out, double *energies,
+                          double *kinetic) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!s->host_stage) {
+        // pinned staging for the energy words and the status word
+        const size_t bytes = sizeof(long long) * (kEnergySlots * (size_t)s->n_sys + 1);
+        CK(cudaMallocHost((void **)&s->host_stage, bytes), "pinned staging");
+    }
+    if (x_in) {
+        CK(cudaMemcpyAsync(s->x, x_in, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice,
+                           s->stream),
+           "copy positions");
+        s->have_x = 1;
+        s->need_reorder = 1;
+        s->forces_valid = 0;
+    }
+    if (v_in) {
+        CK(cudaMemcpyAsync(s->v, v_in, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice,
+                           s->stream),
+           "copy velocities");
+        s->have_v = 1;
+    }
+    const int want_energy = (energies || kinetic) ? 1 : 0;
+    rc = mdg_integrate(s, n_steps, mask, want_energy);
+    if (rc) {
+        cudaStreamSynchronize(s->stream);
+        return rc;
+    }
+    if (x_out) {
+        CK(launch_positions_out(s, s->fout), "positions out");
+        CK(cudaMemcpyAsync(x_out, s->fout, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost,
+                           s->stream),
+           "copy positions");
+    }
+    if (v_out)
+        CK(cudaMemcpyAsync(v_out, s->v, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost,
+                           s->stream),
+           "copy velocities");
+    long long *stage = s->host_stage;
+    const size_t ne = (size_t)kEnergySlots * s->n_sys;
+    if (want_energy)
+        CK(cudaMemcpyAsync(stage, s->energy, sizeof(long long) * ne, cudaMemcpyDeviceToHost,
+                           s->stream),
+           "copy energies");
+    CK(cudaMemcpyAsync(stage + ne, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+       "status read");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    const int st = (int)(stage[ne] & 0xffffffffll);
+    if (st) {
+        CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
+        CK(cudaStreamSynchronize(s->stream), "synchronize");
+        return decode_status(s, st);
+    }
+    const bool recip = (s->forces_mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on;
+    if (energies)
+        for (int t = 0; t < MDG_NUM_TERMS; ++t) {
+            double a = 0.0;
+            for (int q = 0; q < s->n_sys; ++q) {
+                a += (double)stage[(size_t)kEnergySlots * q + t] * kFixInv;
+                if (t == MDG_TERM_COUL_RECIP && recip) a += s->e_self[q] + s->e_net[q];
+            }
+            energies[t] = a;
+        }
+    if (kinetic) {
+        double a = 0.0;
+        for (int q = 0; q < s->n_sys; ++q)
+            a += (double)stage[(size_t)kEnergySlots * q + kSlotKinetic] * kFixInv;
+        *kinetic = a;
+    }
     return MDG_OK;
 }
 
@@ -1004,24 +1348,43 @@ MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_en
     rc = ready_for_forces(s, mask);
     if (rc) return rc;
     if (!s->have_masses) return fail(MDG_ERR_STATE, "masses have not been set");
+    if (s->graph.exec && s->graph.mask != mask) drop_graph(s);
+    for (auto &row : s->graph_step)
+        for (Graph &g : row)
+            if (g.exec && g.mask != mask) drop_graph(s);
+    for (Graph &g : s->graph_eval)
+        if (g.exec && g.mask != mask) drop_graph(s);
     if (!s->forces_valid || s->forces_mask != mask) {
-        rc = evaluate(s, mask, 1);
-        if (rc) return rc;
+        if (s->graph_mode == MDG_GRAPH_STEP && n_steps > 0) {
+            const int resort = s->need_reorder ? 1 : 0;
+            Graph &g = s->graph_eval[resort];
+            if (!g.exec) {
+                rc = capture_eval(s, g, resort, mask);
+                if (rc) return rc;
+            }
+            CK(cudaGraphLaunch(g.exec, s->stream), "graph launch");
+            s->launches += g.steps;
+            if (resort) {
+                s->need_reorder = 0;
+                s->steps_since_reorder = 0;
+            }
+        } else {
+            rc = evaluate(s, mask, 1);
+            if (rc) return rc;
+        }
         s->forces_valid = 1;
         s->forces_mask = mask;
     }
-    if (s->graph.exec && s->graph.mask != mask) drop_graph(s);
-    if (s->graph_step[0].exec && s->graph_step[0].mask != mask) drop_graph(s);
-    if (s->graph_step[1].exec && s->graph_step[1].mask != mask) drop_graph(s);
     const int R = s->reorder_interval;
     int remaining = n_steps;
     while (remaining > 0) {
         const bool chunk_start = s->need_reorder || s->steps_since_reorder >= R;
         const int usable = remaining - (want_energy ? 1 : 0);
-        if (s->graph_mode == MDG_GRAPH_STEP && usable >= 1) {
-            Graph &g = s->graph_step[chunk_start ? 1 : 0];
+        if (s->graph_mode == MDG_GRAPH_STEP) {
+            const int e = (want_energy && remaining == 1) ? 1 : 0;
+            Graph &g = s->graph_step[chunk_start ? 1 : 0][e];
             if (!g.exec) {
-                rc = capture_steps(s, g, 1, chunk_start, mask);
+                rc = capture_steps(s, g, 1, chunk_start, mask, e);
                 if (rc) return rc;
             }
             CK(cudaGraphLaunch(g.exec, s->stream), "graph launch");

@@ -180,7 +180,11 @@ struct mdg_system {
     cudaStream_t own_stream = nullptr, stream = nullptr;
     // side stream for the work that runs beside the pair kernel (PME, special
     // pairs, bonded terms), joined back through two events
-    cudaStream_t side_stream = nullptr;
+    // PME runs on side_stream, special pairs and bonded terms on bond_stream,
+    // both beside the pair kernel; each pair of streams: normal, highest priority
+    cudaStream_t side_stream = nullptr, bond_stream = nullptr;
+    cudaStream_t side_streams[2] = {nullptr, nullptr}, bond_streams[2] = {nullptr, nullptr};
+    cudaEvent_t ev_join2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int n = 0, n_pad = 0, n_clusters = 0;
     std::vector<mdg::SysDev> sys_h;    // host copy of the system table
@@ -234,6 +238,19 @@ struct mdg_system {
     unsigned long long *stats = nullptr;  // 4 counters
     unsigned long long *step_dev = nullptr;
     double *fout = nullptr;            // (n,3) FP64 staging for get_forces
+    long long *host_stage = nullptr;   // pinned host staging of mdg_step_host
+
+    // launch shapes (set by hand or by mdg_autotune): work items per
+    // i-cluster, persistent work-queue form, PME spread/gather block size
+    int nb_split = 4;
+    int nb_persistent = 0;            // 0: one CTA per item; else resident CTAs per SM
+    int nb_persistent_ctas = 0;       // SMs x nb_persistent
+    int n_sms = 0;
+    int *nb_queue = nullptr;
+    int pme_block = 256;
+    int side_priority = 0;            // 1: side stream at the highest priority
+    int nb_split_rings = 1;           // 1: charge-only j atoms sweep without LJ
+    int pme_tiles = 0;                // bit 0: tiled spread, bit 1: tiled gather
 
     // nonbonded configuration
     float cutoff = 12.0f, rswitch = 0.0f;
@@ -269,7 +286,8 @@ struct mdg_system {
     unsigned forces_mask = 0;
     long long launches = 0;
     mdg::Graph graph;                  // chunk of reorder_interval steps
-    mdg::Graph graph_step[2];          // one step: [0] plain, [1] starting with a re-sort
+    mdg::Graph graph_step[2][2];       // one step: [re-sort first][with energies]
+    mdg::Graph graph_eval[2];          // the evaluation before a first step: [re-sort first]
     int graph_mode = 0;
 
     // pair dump

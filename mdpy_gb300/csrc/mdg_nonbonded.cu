@@ -10,7 +10,7 @@
 // and adds the Ewald real-space term k q_i q_j erfc(beta r)/r (MDG_COUL_EWALD),
 // which mdpy v0.2.1 does not have, plus an optional CHARMM switch for LJ.
 //
-// Design (GB300): kSplit = 4 independent single-warp CTAs per 32-atom
+// Design (GB300): `split` (default 4) independent single-warp work items per 32-atom
 // i-cluster I (no block barrier: a warp that finishes early frees its slot).
 //   1. each warp walks its own interleaved batches of cluster bounding boxes
 //      (a balanced half shell: the cluster pair {I, J} belongs to one of the
@@ -33,12 +33,13 @@
 // bit-reproducible run to run.  Pairs are never stored: the pair set is
 // found afresh from the current coordinates on every evaluation, so no
 // Verlet skin or rebuild criterion exists that could miss a pair.
+#include <type_traits>
+
 #include "mdg_internal.cuh"
 
 namespace mdg {
 namespace {
 
-constexpr int kSplit = 4;  // work items (one warp each) per i-cluster
 constexpr int kRing = 64;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -78,6 +79,11 @@ struct NbArgs {
     long long dump_cap;
     unsigned long long *dump_count;
     const int *perm;
+    int split;        // work items (one warp each) per i-cluster
+    int persistent;   // 1: warps pull items from `queue` until none is left
+    int n_items;      // n_clusters * split
+    int *queue;       // next item (zeroed before each persistent launch)
+    int split_rings;  // 1: separate rings for LJ-carrying and charge-only j atoms
 };
 
 __device__ __forceinline__ void decode_shift(int code, const float (&L)[3], float &sx, float &sy,
@@ -87,21 +93,26 @@ __device__ __forceinline__ void decode_shift(int code, const float (&L)[3], floa
     sz = (float)(code % 3 - 1) * L[2];
 }
 
-// one j entry staged in shared memory: shifted coordinates + charge, LJ
-// parameters, cluster-order index, exclusion mask of the 32 i lanes
-struct JEntry {
-    float4 xq;
-    float2 prm;
-    int jk;
-    unsigned mask;
-};
+// One j entry staged in shared memory, two float4: the shifted coordinates
+// + charge, and (sigma/2, sqrt(4 eps), exclusion mask of the 32 i lanes,
+// cluster-order index) -- one 128-bit shared load each in the sweep.
+__device__ __forceinline__ void put_entry(float4 *ring, int pos, float4 xq, float2 prm,
+                                          unsigned mask, int jk) {
+    ring[2 * pos] = xq;
+    ring[2 * pos + 1] = make_float4(prm.x, prm.y, __uint_as_float(mask), __int_as_float(jk));
+}
 
-template <int COUL, bool SWITCH, bool ENERGY, bool DUMP>
-__global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
-    __shared__ JEntry s_j[kRing];
+__device__ __forceinline__ void lds128(unsigned addr, float4 &v) {
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr));
+}
 
-    const int I = blockIdx.x / kSplit;     // i-cluster
-    const int part = blockIdx.x % kSplit;  // which quarter of the candidate scan
+// One work item: part `part` (of a.split) of i-cluster I's pair search.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP>
+__device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int part,
+                                        float4 *s_j) {
+    float4 *const ringL = s_j, *const ringQ = s_j + 2 * kRing;
     const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
     if (cI.w == 0.f) return;  // all-padding cluster
     // this cluster's system: its box, and the range of clusters it may pair with
@@ -122,44 +133,55 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
     float fix = 0.f, fiy = 0.f, fiz = 0.f;
     double acc_lj = 0.0, acc_c = 0.0;  // per-lane energies: FP32 within a chunk, FP64 across
     unsigned long long n_eval = 0, n_in = 0;
-    int jbase = 0, jcount = 0;
+    // two rings: j atoms with LJ parameters, and charge-only j atoms, whose
+    // sweeps skip the LJ arithmetic (two of every three water atoms)
+    int jbL = 0, jcL = 0, jbQ = 0, jcQ = 0;
 
-    // sweep of one 32-entry chunk starting at ring slot `base` (0 or 32)
-    auto chunk = [&](int base) {
+    // Sweep of one 32-entry chunk starting at ring slot `base` (0 or 32).  At
+    // step t lane l pairs its i atom with entry l ^ t and keeps the i force;
+    // the j-force accumulator of entry e travels so that it always sits in
+    // the lane that pairs with e next (a butterfly shuffle with mask
+    // t ^ (t + 1)).  After step 31 lane l owns entry l ^ 31's complete j
+    // force.  The chunk is 1024-byte aligned, so entry l ^ t lives at
+    // (chunk | l << 5) ^ (t << 5): one logic op per step for the address.
+    const unsigned lanebit = 1u << lane;
+    auto chunk = [&](auto with_lj, float4 *ring, int base) {
+        constexpr bool WL = decltype(with_lj)::value;
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(ring + 2 * base);
         float fjx = 0.f, fjy = 0.f, fjz = 0.f;
         float c_lj = 0.f, c_c = 0.f;
-#pragma unroll 4
-        for (int t = 0; t < 32; ++t) {
-            const JEntry &je = s_j[base + ((lane + t) & 31)];
-            const float4 xj = je.xq;
-            const float2 pj = je.prm;
-            const unsigned mk = je.mask;
+        auto step = [&](unsigned addr, unsigned shfl_mask) {
+            float4 xj, aux;
+            lds128(addr, xj);
+            lds128(addr + 16u, aux);
+            const unsigned mk = __float_as_uint(aux.z);
             const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const bool inc = (r2 <= a.rc2) && !((mk >> lane) & 1u);
+            // masked and out-of-range pairs may compute inf/NaN (r2 = 0 for an
+            // atom with itself); every use below selects them away
+            const bool inc = (r2 <= a.rc2) && !(mk & lanebit);
             if (DUMP && inc) {
                 unsigned long long slot = atomicAdd(a.dump_count, 1ull);
                 if ((long long)slot < a.dump_cap) {
-                    int pj_atom = a.perm[je.jk], pi_atom = a.perm[ik];
+                    int pj_atom = a.perm[__float_as_int(aux.w)], pi_atom = a.perm[ik];
                     a.dump[2 * slot] = min(pi_atom, pj_atom);
                     a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
                 }
             }
-            const float r2s = inc ? r2 : 1.0f;
-            const float rinv = rsqrtf(r2s);
+            const float rinv = rsqrtf(r2);
             const float rinv2 = rinv * rinv;
             float fr = 0.f, elj = 0.f, ecl = 0.f;
-            if (a.lj_on) {
-                const float sig = pi.x + pj.x;
+            if (LJ && WL) {
+                const float sig = pi.x + aux.x;
                 const float s2 = sig * sig * rinv2;
                 const float s6 = s2 * s2 * s2;
-                const float c6 = pi.y * pj.y * s6;
+                const float c6 = pi.y * aux.y * s6;
                 float flj = c6 * fmaf(12.0f, s6, -6.0f) * rinv2;
                 if (SWITCH) {
                     // CHARMM switch, branch free: below rs the clamped r^2 gives
                     // sw = 1 and dsw = 0 exactly
                     elj = c6 * (s6 - 1.0f);
-                    const float r2c = fmaxf(r2s, a.rs2);
+                    const float r2c = fmaxf(r2, a.rs2);
                     const float u = a.rc2 - r2c;
                     const float sw = u * u * fmaf(2.0f, r2c, a.rc2 - 3.0f * a.rs2) * a.sw_inv_den;
                     const float dsw = 12.0f * u * (a.rs2 - r2c) * a.sw_inv_den;
@@ -172,11 +194,11 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
             }
             if (COUL == MDG_COUL_EWALD) {
                 const float qq = xi.w * xj.w;
-                const float r = r2s * rinv;
+                const float r = r2 * rinv;
                 const float tt = __fdividef(1.0f, fmaf(a.beta_p, r, 1.0f));
                 const float poly =
                     tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, kAsA5, kAsA4), kAsA3), kAsA2), kAsA1);
-                const float ex = exp2f(-a.ewald_exp_c * r2s);
+                const float ex = exp2f(-a.ewald_exp_c * r2);
                 const float ecf = qq * poly * ex * rinv;
                 fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecf), rinv2, fr);
                 // the force keeps the 1.5e-7 approximation in every variant (so a
@@ -197,12 +219,23 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
                 c_c += inc ? ecl : 0.f;
                 n_in += __popc(__ballot_sync(kFull, inc));
             }
-            const int src = (lane + 1) & 31;
-            fjx = __shfl_sync(kFull, fjx, src);
-            fjy = __shfl_sync(kFull, fjy, src);
-            fjz = __shfl_sync(kFull, fjz, src);
+            fjx = __shfl_xor_sync(kFull, fjx, shfl_mask);
+            fjy = __shfl_xor_sync(kFull, fjy, shfl_mask);
+            fjz = __shfl_xor_sync(kFull, fjz, shfl_mask);
+        };
+#pragma unroll 1
+        for (int t0 = 0; t0 < 32; t0 += 4) {
+            const unsigned sb = sa | ((unsigned)(lane ^ t0) << 5);
+            // masks t ^ (t + 1) for t = t0 .. t0 + 3; none after the last step
+            const unsigned m3 = t0 == 28 ? 0u : (unsigned)((t0 + 3) ^ (t0 + 4));
+            step(sb, 1u);
+            step(sb ^ 32u, 3u);
+            step(sb ^ 64u, 1u);
+            step(sb ^ 96u, m3);
         }
-        const int jk = s_j[base + lane].jk;
+        float4 own;
+        lds128(sa + ((unsigned)(lane ^ 31) << 5) + 16u, own);
+        const int jk = __float_as_int(own.w);
         if (jk >= 0 && !DUMP) {
             if (!(fabsf(fjx) < kFixLimit && fabsf(fjy) < kFixLimit && fabsf(fjz) < kFixLimit))
                 raise_status(a.status, MDG_ERR_OVERFLOW);
@@ -232,9 +265,16 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
         const float gy = fmaxf(fabsf(xj.y - cI.y) - hI.y, 0.f);
         const float gz = fmaxf(fabsf(xj.z - cI.z) - hI.z, 0.f);
         const bool hit = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) <= a.rc2;
-        const unsigned b = __ballot_sync(kFull, hit);
-        if (b == 0u) return;
-        if (hit) {
+        const float2 pj = hit ? a.prm[jk] : make_float2(0.f, 0.f);
+        // With split rings, LJ-carrying atoms go to ring L and the rest,
+        // which matter only for the Ewald term (or the pair-set dump), to
+        // ring Q; otherwise every hit goes to ring L.
+        const bool to_l = !a.split_rings || (LJ && pj.y != 0.f);
+        const bool hitL = hit && to_l;
+        const bool hitQ = hit && !to_l && (COUL == MDG_COUL_EWALD || DUMP);
+        const unsigned bL = __ballot_sync(kFull, hitL), bQ = __ballot_sync(kFull, hitQ);
+        if ((bL | bQ) == 0u) return;
+        if (hitL || hitQ) {
             unsigned m = 0u;
             if (J == I) m = kFull << lane;  // half shell inside the cluster
             if (rI.y >= J * kCluster && rI.x < (J + 1) * kCluster) {
@@ -246,25 +286,26 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
                     }
                 }
             }
-            const int pos = (jbase + jcount + __popc(b & lt)) & (kRing - 1);
-            JEntry e;
-            e.xq = xj;
-            e.prm = a.prm[jk];
-            e.jk = jk;
-            e.mask = m;
-            s_j[pos] = e;
+            if (hitL) put_entry(ringL, (jbL + jcL + __popc(bL & lt)) & (kRing - 1), xj, pj, m, jk);
+            else put_entry(ringQ, (jbQ + jcQ + __popc(bQ & lt)) & (kRing - 1), xj, pj, m, jk);
         }
-        jcount += __popc(b);
+        jcL += __popc(bL);
+        jcQ += __popc(bQ);
         __syncwarp();
-        if (jcount >= 32) {
-            chunk(jbase);
-            jbase = (jbase + 32) & (kRing - 1);
-            jcount -= 32;
+        if (jcL >= 32) {
+            chunk(std::true_type{}, ringL, jbL);
+            jbL = (jbL + 32) & (kRing - 1);
+            jcL -= 32;
+        }
+        if (jcQ >= 32) {
+            chunk(std::false_type{}, ringQ, jbQ);
+            jbQ = (jbQ + 32) & (kRing - 1);
+            jcQ -= 32;
         }
     };
 
-    // Candidate clusters.  Work item `part` scans batches part, part + kSplit,
-    // ... of 32 clusters, so the kSplit warps of one i-cluster share its
+    // Candidate clusters.  Work item `part` scans batches part, part + split,
+    // ... of 32 clusters, so the split warps of one i-cluster share its
     // neighbourhood without talking to each other.
     // Balanced half shell: the cluster pair {I, J} (I != J) belongs to I when
     // I < J and I + J is odd, or when I > J and I + J is even -- every cluster
@@ -325,7 +366,7 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
                 if (lane >= o) incl += t;
             }
             const int total = __shfl_sync(kFull, incl, 31);
-            for (int v0 = part * 32; v0 < total; v0 += kSplit * 32) {
+            for (int v0 = part * 32; v0 < total; v0 += a.split * 32) {
                 const int v = v0 + lane;
                 int lo = 0, hi = 31;  // first lane whose inclusive count exceeds v
 #pragma unroll
@@ -377,8 +418,8 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
         }
     } else {
         // full scan of the system's clusters: work item `part` takes batches
-        // part, part + kSplit, ... of 32 clusters
-        for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += kSplit * 32) {
+        // part, part + split, ... of 32 clusters
+        for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += a.split * 32) {
             const int J = J0 + lane;
             bool valid = J < cl_hi && owned(J);
             float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
@@ -426,18 +467,34 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
             }
         }
     }
-    if (jcount > 0) {
-        const int pos = (jbase + lane) & (kRing - 1);
-        if (lane >= jcount) {
-            JEntry e;
-            e.xq = make_float4(kFarAway, kFarAway, kFarAway, 0.f);
-            e.prm = make_float2(0.f, 0.f);
-            e.jk = -1;
-            e.mask = kFull;
-            s_j[pos] = e;
+    // The partial last chunks, padded with far-away entries.  When both fit
+    // in one chunk the charge-only entries join the LJ chunk (their LJ terms
+    // are zero), so an item ends with at most one partial sweep.
+    if (jcQ > 0 && jcL + jcQ <= 32) {
+        if (lane < jcQ) {
+            const float4 *src = ringQ + 2 * ((jbQ + lane) & (kRing - 1));
+            float4 *dst = ringL + 2 * ((jbL + jcL + lane) & (kRing - 1));
+            const float4 e0 = src[0], e1 = src[1];
+            dst[0] = e0;
+            dst[1] = e1;
         }
+        jcL += jcQ;
+        jcQ = 0;
         __syncwarp();
-        chunk(jbase);
+    }
+    if (jcL > 0) {
+        if (lane >= jcL)
+            put_entry(ringL, (jbL + lane) & (kRing - 1), make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                      make_float2(0.f, 0.f), kFull, -1);
+        __syncwarp();
+        chunk(std::true_type{}, ringL, jbL);
+    }
+    if (jcQ > 0) {
+        if (lane >= jcQ)
+            put_entry(ringQ, (jbQ + lane) & (kRing - 1), make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                      make_float2(0.f, 0.f), kFull, -1);
+        __syncwarp();
+        chunk(std::false_type{}, ringQ, jbQ);
     }
 
     // ---- this work item's share of the i forces and energies -------------
@@ -461,6 +518,29 @@ __global__ void __launch_bounds__(32, 24) k_nonbonded(NbArgs a) {
             atomicAdd(&a.stats[2], (unsigned long long)n_cand);
             if (part == 0) atomicAdd(&a.stats[3], 1ull);
         }
+    }
+}
+
+// Grid form: one one-warp CTA per work item, scheduled by the hardware.
+// Persistent form: enough warps to fill the GPU once, each pulling work
+// items from a device counter until none is left.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP>
+__global__ void __launch_bounds__(32, ENERGY ? 16 : 24) k_nonbonded(NbArgs a) {
+    // two rings of 64 entries of 32 bytes; each 32-entry chunk starts on a
+    // 1024-byte boundary
+    __shared__ __align__(1024) float4 s_j[4 * kRing];
+    if (!a.persistent) {
+        nb_item<COUL, LJ, SWITCH, ENERGY, DUMP>(a, blockIdx.x / a.split, blockIdx.x % a.split,
+                                                s_j);
+        return;
+    }
+    for (;;) {
+        int item = 0;
+        if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
+        item = __shfl_sync(kFull, item, 0);
+        if (item >= a.n_items) break;
+        __syncwarp();  // the previous item's ring reads are done
+        nb_item<COUL, LJ, SWITCH, ENERGY, DUMP>(a, item / a.split, item % a.split, s_j);
     }
 }
 
@@ -672,18 +752,25 @@ NbArgs make_args(mdg_system *s) {
     a.dump_cap = s->dump_cap;
     a.dump_count = s->dump_count;
     a.perm = s->perm;
+    a.split = s->nb_split;
+    a.persistent = s->nb_persistent > 0;
+    a.n_items = s->n_clusters * s->nb_split;
+    a.queue = s->nb_queue;
+    a.split_rings = s->nb_split_rings;
     return a;
 }
 
-template <int COUL, bool SW>
+template <int COUL, bool LJ, bool SW>
 cudaError_t dispatch_nb(mdg_system *s, const NbArgs &a, int energy, int dump) {
-    dim3 grid(s->n_clusters * kSplit), block(32);
+    dim3 grid(a.persistent ? s->nb_persistent_ctas : a.n_items), block(32);
+    if (a.persistent && cudaMemsetAsync(a.queue, 0, sizeof(int), s->stream) != cudaSuccess)
+        return cudaGetLastError();
     if (dump)
-        k_nonbonded<COUL, SW, false, true><<<grid, block, 0, s->stream>>>(a);
+        k_nonbonded<COUL, LJ, SW, false, true><<<grid, block, 0, s->stream>>>(a);
     else if (energy)
-        k_nonbonded<COUL, SW, true, false><<<grid, block, 0, s->stream>>>(a);
+        k_nonbonded<COUL, LJ, SW, true, false><<<grid, block, 0, s->stream>>>(a);
     else
-        k_nonbonded<COUL, SW, false, false><<<grid, block, 0, s->stream>>>(a);
+        k_nonbonded<COUL, LJ, SW, false, false><<<grid, block, 0, s->stream>>>(a);
     return cudaGetLastError();
 }
 
@@ -699,12 +786,14 @@ cudaError_t launch_nonbonded(mdg_system *s, unsigned mask, int energy, int dump)
     cudaError_t err = cudaSuccess;
     const int coul_tile = (want_c && s->coul_mode == MDG_COUL_EWALD) ? MDG_COUL_EWALD : MDG_COUL_NONE;
     if (want_lj || coul_tile == MDG_COUL_EWALD) {
-        if (coul_tile == MDG_COUL_EWALD)
-            err = sw ? dispatch_nb<MDG_COUL_EWALD, true>(s, a, energy, dump)
-                     : dispatch_nb<MDG_COUL_EWALD, false>(s, a, energy, dump);
+        if (coul_tile == MDG_COUL_EWALD && !want_lj)
+            err = dispatch_nb<MDG_COUL_EWALD, false, false>(s, a, energy, dump);
+        else if (coul_tile == MDG_COUL_EWALD)
+            err = sw ? dispatch_nb<MDG_COUL_EWALD, true, true>(s, a, energy, dump)
+                     : dispatch_nb<MDG_COUL_EWALD, true, false>(s, a, energy, dump);
         else
-            err = sw ? dispatch_nb<MDG_COUL_NONE, true>(s, a, energy, dump)
-                     : dispatch_nb<MDG_COUL_NONE, false>(s, a, energy, dump);
+            err = sw ? dispatch_nb<MDG_COUL_NONE, true, true>(s, a, energy, dump)
+                     : dispatch_nb<MDG_COUL_NONE, true, false>(s, a, energy, dump);
         s->launches += 1;
         if (err != cudaSuccess) return err;
     }

@@ -55,6 +55,10 @@ class DumperPoorDefinedError(Exception):
     pass
 
 
+class FileFormatError(Exception):
+    pass
+
+
 class ParticleLossError(Exception):
     pass
 

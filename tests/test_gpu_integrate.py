@@ -158,3 +158,42 @@ def test_nve_energy_conservation(lib):
     assert np.all(np.isfinite(e))
     # drift over 250 fs well below the kinetic energy scale
     assert abs(e[-1] - e[0]) < 2e-3 * ke
+
+
+def test_step_host_equals_separate_calls(lib):
+    """mdg_step_host (copies in, n steps, copies out, one synchronisation)
+    gives bit for bit what the separate set / integrate / get calls give."""
+    from mdpy_gb300 import systems
+    from tests.helpers import make_system, water_lj_rows
+
+    w = systems.water_box(600, 26.0, seed=12)
+    t = w.topology
+    mask = lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL, lib.TERM_COUL_RECIP)
+
+    def build():
+        s = make_system(lib, w.num_particles, w.box, masses=t.masses.reshape(-1),
+                        charges=t.charges.reshape(-1), lj=water_lj_rows(w),
+                        bonded=t.bonded_particles, cutoff=10.0, coulomb=lib.COUL_EWALD,
+                        beta=0.3, positions=w.positions)
+        s.pme_config(27, 4, 0.3)
+        s.integrator_config(lib.INTEGRATOR_LANGEVIN, 1.0, 300.0, 0.001, 5)
+        return s
+
+    a, b = build(), build()
+    x = np.ascontiguousarray(w.positions + 0.01)
+    v = np.ascontiguousarray(w.velocities)
+    a.set_positions(x)
+    a.set_velocities(v)
+    a.integrate(7, mask, want_energy=True)
+    xa, va = a.get_positions(), a.get_velocities()
+    ea, kea = a.get_energies()
+    xb, vb = np.empty_like(x), np.empty_like(v)
+    eb = np.zeros(lib.NUM_TERMS)
+    keb = b.step_host_ptr(x.ctypes.data, v.ctypes.data, 7, mask, xb.ctypes.data, vb.ctypes.data,
+                          eb)
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    assert np.array_equal(ea, eb) and kea == keb
+    # outputs only: the state carries on from where it was
+    keb2 = b.step_host_ptr(0, 0, 3, mask, xb.ctypes.data, 0, eb)
+    a.integrate(3, mask, want_energy=True)
+    assert np.array_equal(a.get_positions(), xb) and a.get_energies()[1] == keb2

@@ -190,3 +190,35 @@ def test_ensemble_batch_concatenates_member_setup(monkeypatch):
                           C.CharmmBondConstraint(ws[1].parameters["bond"]))
     with pytest.raises(ValueError, match="disagree"):
         batch.EnsembleBatch([members[0], other])
+
+
+def test_pdb_dumper_writes_fixed_column_frames(tmp_path):
+    """PDBDumper on a stand-in simulation: CRYST1 once, one MODEL per dump,
+    coordinates in columns 31-54 as the PDB format fixes them."""
+    from types import SimpleNamespace
+
+    from mdpy_gb300 import systems
+    from mdpy_gb300.dumper import PDBDumper
+    from mdpy_gb300.error import DumperPoorDefinedError, FileFormatError
+
+    w = systems.water_box(20, 12.0, seed=1)
+    frames = [w.positions - 6.0, w.positions - 5.5]
+    state = SimpleNamespace(pbc_matrix=np.diag(w.box), positions=None)
+    sim = SimpleNamespace(ensemble=SimpleNamespace(topology=w.topology, state=state))
+    with pytest.raises(FileFormatError):
+        PDBDumper(str(tmp_path / "x.txt"), 1)
+    with pytest.raises(DumperPoorDefinedError):
+        PDBDumper(str(tmp_path / "x.pdb"), 0)
+    d = PDBDumper(str(tmp_path / "t.pdb"), 10)
+    for x in frames:
+        state.positions = x
+        d.dump(sim)
+    d.close()
+    lines = open(tmp_path / "t.pdb").read().splitlines()
+    assert lines[0].startswith("CRYST1") and float(lines[0][6:15]) == pytest.approx(12.0)
+    assert sum(ln.startswith("MODEL") for ln in lines) == 2
+    atoms = [ln for ln in lines if ln.startswith("ATOM")]
+    assert len(atoms) == 2 * 60
+    xyz = np.array([[float(ln[30:38]), float(ln[38:46]), float(ln[46:54])] for ln in atoms])
+    assert np.allclose(xyz, np.concatenate(frames), atol=5e-4)
+    assert atoms[1][12:16].strip() == "HT" and int(atoms[59][6:11]) == 60
