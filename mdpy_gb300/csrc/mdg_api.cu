@@ -106,6 +106,7 @@ int validate_boxes(mdg_system *s, double cutoff) {
 void set_sys_box(SysDev &d, const double *box) {
     for (int k = 0; k < 3; ++k) {
         d.Ld[k] = box[k];
+        d.invLd[k] = 1.0 / box[k];
         d.L[k] = (float)box[k];
         d.invL[k] = (float)(1.0 / box[k]);
     }

@@ -46,12 +46,12 @@ struct BdArgs {
 };
 
 __device__ __forceinline__ float3 mind(const BdArgs &a, int i, int j) {
-    const double *L = a.sys[a.atom_sys[i]].Ld;  // a term never spans two systems
+    const SysDev &sd = a.sys[a.atom_sys[i]];  // a term never spans two systems
     double d[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         d[k] = a.x[3 * j + k] - a.x[3 * i + k];
-        d[k] -= L[k] * rint(d[k] / L[k]);
+        d[k] -= sd.Ld[k] * rint(d[k] * sd.invLd[k]);
     }
     return make_float3((float)d[0], (float)d[1], (float)d[2]);
 }

@@ -132,6 +132,7 @@ __device__ void block_energy_add(long long *energy, int sys, const double (&v)[N
 struct SysDev {
     float L[3], invL[3];    // box edges (A) and inverses
     double Ld[3];           // FP64 box for the FP64 minimum image
+    double invLd[3];        // and its inverse (GB300's FP64 divide is slow)
     int atom_off, n_atoms;  // atom range
     int cl_off, cl_cap;     // cluster range (capacity: ceil(n/32) + columns)
     int col_off, n_cols;    // sort columns

@@ -150,10 +150,7 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         const unsigned sa = (unsigned)__cvta_generic_to_shared(ring + 2 * base);
         float fjx = 0.f, fjy = 0.f, fjz = 0.f;
         float c_lj = 0.f, c_c = 0.f;
-        auto step = [&](unsigned addr, unsigned shfl_mask) {
-            float4 xj, aux;
-            lds128(addr, xj);
-            lds128(addr + 16u, aux);
+        auto step = [&](const float4 &xj, const float4 &aux, unsigned shfl_mask) {
             const unsigned mk = __float_as_uint(aux.z);
             const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -223,15 +220,31 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
             fjy = __shfl_xor_sync(kFull, fjy, shfl_mask);
             fjz = __shfl_xor_sync(kFull, fjz, shfl_mask);
         };
+        // each step's entry is loaded one step ahead, so its shared-memory
+        // latency overlaps the previous step's arithmetic
+        float4 xa, aa, xb, ab;
+        lds128(sa | ((unsigned)lane << 5), xa);
+        lds128((sa | ((unsigned)lane << 5)) + 16u, aa);
 #pragma unroll 1
         for (int t0 = 0; t0 < 32; t0 += 4) {
             const unsigned sb = sa | ((unsigned)(lane ^ t0) << 5);
             // masks t ^ (t + 1) for t = t0 .. t0 + 3; none after the last step
             const unsigned m3 = t0 == 28 ? 0u : (unsigned)((t0 + 3) ^ (t0 + 4));
-            step(sb, 1u);
-            step(sb ^ 32u, 3u);
-            step(sb ^ 64u, 1u);
-            step(sb ^ 96u, m3);
+            lds128(sb ^ 32u, xb);
+            lds128((sb ^ 32u) + 16u, ab);
+            step(xa, aa, 1u);
+            lds128(sb ^ 64u, xa);
+            lds128((sb ^ 64u) + 16u, aa);
+            step(xb, ab, 3u);
+            lds128(sb ^ 96u, xb);
+            lds128((sb ^ 96u) + 16u, ab);
+            step(xa, aa, 1u);
+            if (t0 < 28) {
+                const unsigned nb = sa | ((unsigned)(lane ^ (t0 + 4)) << 5);
+                lds128(nb, xa);
+                lds128(nb + 16u, aa);
+            }
+            step(xb, ab, m3);
         }
         float4 own;
         lds128(sa + ((unsigned)(lane ^ 31) << 5) + 16u, own);
@@ -525,7 +538,7 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
 // Persistent form: enough warps to fill the GPU once, each pulling work
 // items from a device counter until none is left.
 template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP>
-__global__ void __launch_bounds__(32, ENERGY ? 16 : 24) k_nonbonded(NbArgs a) {
+__global__ void __launch_bounds__(32, ENERGY ? 16 : 20) k_nonbonded(NbArgs a) {
     // two rings of 64 entries of 32 bytes; each 32-entry chunk starts on a
     // 1024-byte boundary
     __shared__ __align__(1024) float4 s_j[4 * kRing];
@@ -644,12 +657,12 @@ __global__ void k_special(SpArgs a) {
         const int2 pr = is14 ? a.p14[t - a.n_excl] : a.excl[t];
         const int i = pr.x, j = pr.y;
         sid = a.atom_sys[i];
-        const double *Ld = a.sys[sid].Ld;
+        const SysDev &sd = a.sys[sid];
         float d[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             double dd = a.x[3 * j + k] - a.x[3 * i + k];
-            dd -= Ld[k] * rint(dd / Ld[k]);
+            dd -= sd.Ld[k] * rint(dd * sd.invLd[k]);
             d[k] = (float)dd;
         }
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
