@@ -591,16 +591,37 @@ def main():
     peak_src = "measured" if hbm_peak else "fallback"
     hbm_peak = hbm_peak or 6800.0
     traffic = None
+    issue = None
+    pairs_in = stats["pairs_in_cutoff"]
     if os.path.exists(PROFILE_INPUTS):
         with open(PROFILE_INPUTS) as fh:
-            traffic = json.load(fh).get("nonbonded_dram_bytes_per_launch")
+            prof = json.load(fh)
+        # one ncu capture of the 88k box; other sizes scale by the units processed
+        traffic = prof["nonbonded_dram_bytes_per_launch"] * alg_bytes / prof["alg_bytes_per_launch"]
+        inst = (prof["warp_instructions_per_launch"] * stats["pair_evaluations"]
+                / prof["pair_evaluations_per_launch"])
+        # the binding limit of this kernel: warp-instruction issue (4 schedulers
+        # per SM, one instruction per clock each) at the sampled SM clock
+        sm_mhz = None
+        try:
+            sm_mhz = float(clk.get("sm_mhz")) if clk and clk.get("sm_mhz") else None
+        except (TypeError, ValueError):
+            sm_mhz = None
+        sm_mhz = sm_mhz or 2070.0
+        n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+        peak_issue = n_sms * 4 * sm_mhz * 1e6
+        issue = {"warp_instructions_per_launch": inst, "achieved_per_s": inst / t_nb,
+                 "peak_per_s": peak_issue, "frac": inst / t_nb / peak_issue,
+                 "source": "instructions per pair evaluation from the ncu capture in "
+                           "profiles/roofline_inputs.json x this launch's evaluations; "
+                           "peak = SMs x 4 schedulers x sampled SM clock"}
     achieved = alg_bytes / t_nb / 1e9
-    pairs_in = stats["pairs_in_cutoff"]
     flops = 60.0 * pairs_in / t_nb / 1e12
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "k_nonbonded",
                 "peak_source": peak_src, "alg_bytes_per_launch": alg_bytes,
                 "launch_ms": stage_ms["nonbonded"],
+                "issue": issue,
                 "fp32": {"achieved_tflops": flops, "nominal_peak_tflops": FP32_PEAK_TFLOPS_NOMINAL,
                          "frac": flops / FP32_PEAK_TFLOPS_NOMINAL,
                          "flops_per_pair": 60, "pairs_in_cutoff": pairs_in,

@@ -197,7 +197,10 @@ MDG_API int mdg_step_host(mdg_system *sys, const double *x_in, const double *v_i
  *                              that skip the LJ arithmetic (default 1);
  *   [MDG_SHAPE_PME_TILES]      bit 0: spreading through a shared-memory tile of
  *                              the block's grid patch, bit 1: gathering from one
- *                              (default 0).
+ *                              (default 0);
+ *   [MDG_SHAPE_HALF]           1: each half warp sweeps its own j list against 16
+ *                              i atoms (j atoms within rc of those 16 only), 0:
+ *                              one list against all 32 (default 0).
  * Results depend on the shape only through float rounding of partial sums
  * (the PME grid and tiling change nothing: int64 sums); for a fixed shape
  * they are bit-reproducible. */
@@ -207,14 +210,15 @@ MDG_API int mdg_step_host(mdg_system *sys, const double *x_in, const double *v_i
 #define MDG_SHAPE_SIDE_PRIORITY 3
 #define MDG_SHAPE_SPLIT_RINGS 4
 #define MDG_SHAPE_PME_TILES 5
-#define MDG_SHAPE_FIELDS 6
+#define MDG_SHAPE_HALF 6
+#define MDG_SHAPE_FIELDS 7
 MDG_API int mdg_set_launch_shape(mdg_system *sys, const int *shape);
 MDG_API int mdg_get_launch_shape(mdg_system *sys, int *shape);
 /* Picks the fastest launch shape: with an integrator configured it times MD
  * steps as mdg_integrate runs them (captured single-step graphs replayed from
  * a saved state, which is restored afterwards), else force evaluations of
  * `mask`.  Phase one varies the pair kernel (split 2/4/8 x persistent 0/20/24
- * x split rings 0/1), phase two PME and the streams (block 64/128/256 x tiles
+ * x split rings 0/1 x half 0/1), phase two PME and the streams (block 64/128/256 x tiles
  * 0-3 x side priority 0/1) around phase one's best; then the four fastest and
  * the shape in use are re-timed, interleaved, over 4 x reps and the fastest
  * is kept; *best_ms (may be NULL) receives its time.  Leaves no valid force

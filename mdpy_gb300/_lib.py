@@ -315,20 +315,20 @@ class System:
         return e, ke.value
 
     SHAPE_FIELDS = ("split", "persistent", "pme_block", "side_priority", "split_rings",
-                    "pme_tiles")
+                    "pme_tiles", "half")
 
     def set_launch_shape(self, split=4, persistent=0, pme_block=256, side_priority=0,
-                         split_rings=1, pme_tiles=0):
+                         split_rings=1, pme_tiles=0, half=0):
         """``persistent``: 0 = one CTA per pair work item, n = n resident CTAs
         per SM pulling work items; ``pme_tiles``: bit 0 tiled spreading, bit 1
-        tiled gathering."""
-        sh = (ctypes.c_int * 6)(int(split), int(persistent), int(pme_block), int(side_priority),
-                                int(split_rings), int(pme_tiles))
+        tiled gathering; ``half``: 16-atom i groups per half warp."""
+        sh = (ctypes.c_int * 7)(int(split), int(persistent), int(pme_block), int(side_priority),
+                                int(split_rings), int(pme_tiles), int(half))
         check(self._lib.mdg_set_launch_shape(self._h, sh))
 
     @property
     def launch_shape(self):
-        sh = (ctypes.c_int * 6)()
+        sh = (ctypes.c_int * 7)()
         check(self._lib.mdg_get_launch_shape(self._h, sh))
         return dict(zip(self.SHAPE_FIELDS, list(sh)))
 

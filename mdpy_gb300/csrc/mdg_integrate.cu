@@ -69,10 +69,8 @@ __device__ __forceinline__ double fget(const unsigned long long *f, int k) {
     return (double)(long long)f[k] * kFixInv;
 }
 
-__global__ void __launch_bounds__(256) k_pre(InArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    const int k = a.inv_perm[i];
+// the pre-force update of atom i (cluster slot k) from the forces in slot k
+__device__ __forceinline__ void pre_kick(const InArgs &a, int i, int k) {
     const double im = a.inv_mass[i];
     const double F[3] = {fget(a.f, k), fget(a.f, a.n_pad + k), fget(a.f, 2 * a.n_pad + k)};
     double bt[3] = {0.0, 0.0, 0.0};
@@ -97,6 +95,13 @@ __global__ void __launch_bounds__(256) k_pre(InArgs a) {
     }
     if (!ok) raise_status(a.status, MDG_ERR_PARTICLE_LOSS);
 }
+
+__global__ void __launch_bounds__(256) k_pre(InArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    pre_kick(a, i, a.inv_perm[i]);
+}
+
 
 template <bool ENERGY>
 __global__ void __launch_bounds__(256) k_post(InArgs a) {

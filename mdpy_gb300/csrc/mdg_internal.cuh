@@ -127,6 +127,24 @@ __device__ void block_energy_add(long long *energy, int sys, const double (&v)[N
     }
 }
 
+struct SysDev;
+
+// Per-step packing of one 32-slot cluster into the float copy the force
+// kernels read (see pack_cluster below).
+struct PackArgs {
+    const double *x;
+    const int *perm;
+    const float *q_sorted;
+    int n_clusters, n_pad;
+    float4 *xq;
+    float4 *bbox;
+    float4 *hbox;   // boxes of the two 16-slot halves: centre, half extents (x2)
+    unsigned long long *f;
+    const SysDev *sys;
+    const int *cl_sys, *cl_col, *col_xy;
+    float *overhang;
+};
+
 // per-system parameters, read by kernels through a device table (one entry
 // per independent system of a batch; a single system is a batch of one)
 struct SysDev {
@@ -166,6 +184,84 @@ struct Pme {
     float *influence = nullptr;   // influence functions, complex-grid layout
     std::vector<PmeGroup> groups;
 };
+
+// One warp packs cluster `warp`; lane slot k holds atom position c (FP64)
+// when valid.  Writes the float copy (x, y, z, q sqrt(k_e)), zeroes the
+// slot's force words, and lane 0 writes the cluster box and raises the
+// system's overhang (how far boxes reach out of their sort columns).
+// Between re-sorts the FP64 positions drift freely out of [0, L).  The pair
+// search tries the images -1, 0, +1 of each cluster pair, which is exact
+// while every stored coordinate stays within a window of width 1.5 L: a
+// coordinate that leaves [-L/4, 5L/4) is wrapped back into [0, L) here (its
+// cluster box then spans the box, and the search covers it with all 27
+// images).
+__device__ __forceinline__ void pack_cluster(const PackArgs &a, int warp, int k, bool valid,
+                                             double (&c)[3]) {
+    const int lane = threadIdx.x & 31;
+    float4 p;
+    if (valid) {
+        const double *Ld = a.sys[a.cl_sys[warp]].Ld;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (c[d] < -0.25 * Ld[d] || c[d] >= 1.25 * Ld[d]) c[d] -= Ld[d] * floor(c[d] / Ld[d]);
+        p = make_float4((float)c[0], (float)c[1], (float)c[2], a.q_sorted[k]);
+    } else {
+        p = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+    }
+    a.xq[k] = p;
+    a.f[k] = 0ull;
+    a.f[a.n_pad + k] = 0ull;
+    a.f[2 * a.n_pad + k] = 0ull;
+    float lox = valid ? p.x : INFINITY, loy = valid ? p.y : INFINITY, loz = valid ? p.z : INFINITY;
+    float hix = valid ? p.x : -INFINITY, hiy = valid ? p.y : -INFINITY,
+          hiz = valid ? p.z : -INFINITY;
+    const unsigned vb = __ballot_sync(0xffffffffu, valid);
+    // the two 16-slot halves first, then the whole cluster
+#pragma unroll
+    for (int o = 1; o <= 16; o <<= 1) {
+        lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
+        loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, o));
+        loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, o));
+        hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
+        hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
+        hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
+        if (o == 8 && (lane & 15) == 0) {
+            const int h = lane >> 4;
+            const bool any = (vb >> (16 * h)) & 0xffffu;
+            a.hbox[4 * warp + 2 * h] =
+                any ? make_float4(0.5f * (lox + hix), 0.5f * (loy + hiy), 0.5f * (loz + hiz), 1.0f)
+                    : make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+            a.hbox[4 * warp + 2 * h + 1] =
+                any ? make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy), 0.5f * (hiz - loz), 0.0f)
+                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+    const int cnt = __popc(vb);
+    if (lane == 0) {
+        if (cnt == 0) {  // an all-padding cluster: far away, zero extent
+            a.bbox[2 * warp] = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+            a.bbox[2 * warp + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            a.bbox[2 * warp] = make_float4(0.5f * (lox + hix), 0.5f * (loy + hiy),
+                                           0.5f * (loz + hiz), (float)cnt);
+            a.bbox[2 * warp + 1] = make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy),
+                                               0.5f * (hiz - loz), 0.0f);
+            const int col = a.cl_col[warp];
+            if (col >= 0) {
+                const int q = a.cl_sys[warp];
+                const SysDev &d = a.sys[q];
+                const int pk = a.col_xy[col];
+                const float ax = d.L[0] / (float)d.ncx, ay = d.L[1] / (float)d.ncy;
+                const float x0 = (float)(pk >> 16) * ax, y0 = (float)(pk & 0xffff) * ay;
+                const float ov = fmaxf(fmaxf(fmaxf(x0 - lox, hix - (x0 + ax)),
+                                             fmaxf(y0 - loy, hiy - (y0 + ay))),
+                                       0.0f);
+                if (ov > a.overhang[q])
+                    atomicMax((unsigned int *)&a.overhang[q], __float_as_uint(ov));
+            }
+        }
+    }
+}
 
 struct Graph {
     cudaGraphExec_t exec = nullptr;
@@ -234,6 +330,7 @@ struct mdg_system {
     unsigned long long *f = nullptr;   // 3 * n_pad fixed point
     float4 *xq = nullptr;
     float4 *bbox = nullptr;
+    float4 *hbox = nullptr;            // float4[4][clusters]: boxes of the 16-slot halves
     long long *energy = nullptr;       // kEnergySlots per system
     int *status = nullptr;
     unsigned long long *stats = nullptr;  // 4 counters
@@ -252,6 +349,7 @@ struct mdg_system {
     int side_priority = 0;            // 1: side stream at the highest priority
     int nb_split_rings = 1;           // 1: charge-only j atoms sweep without LJ
     int pme_tiles = 0;                // bit 0: tiled spread, bit 1: tiled gather
+    int nb_half = 0;                  // 1: 16-atom i groups per half warp
 
     // nonbonded configuration
     float cutoff = 12.0f, rswitch = 0.0f;
@@ -302,6 +400,7 @@ namespace mdg {
 // each returns cudaError_t of the launch
 cudaError_t launch_reorder(mdg_system *s);
 cudaError_t launch_pack(mdg_system *s);
+PackArgs make_pack_args(mdg_system *s);
 cudaError_t launch_nonbonded(mdg_system *s, unsigned mask, int energy, int dump);
 cudaError_t launch_special(mdg_system *s, unsigned mask, int energy, int dump);
 cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status);

@@ -1,0 +1,654 @@
+// mdg_nonbonded_kernel.cuh -- the pair kernel's templates, shared by the
+// two translation units that instantiate them (whole-warp and half-warp i
+// groups), so that the library builds in parallel.
+#pragma once
+
+#include <type_traits>
+
+#include "mdg_internal.cuh"
+
+namespace mdg {
+
+struct NbArgs {
+    const float4 *__restrict__ xq;
+    const float2 *__restrict__ prm;
+    const int *__restrict__ partners;
+    int pw;
+    const int2 *__restrict__ prange;
+    const float4 *__restrict__ bbox;
+    const SysDev *__restrict__ sys;
+    const int *__restrict__ cl_sys;
+    const float4 *__restrict__ hbox;       // boxes of each cluster's two 16-slot halves
+    const int *__restrict__ cl_col;        // cluster -> global sort column
+    const int *__restrict__ col_xy;        // global column -> (cx << 16) | cy
+    const int *__restrict__ col_rank;      // system column (cx * ncy + cy) -> rank
+    const int *__restrict__ col_cl_start;  // global column -> first cluster (scan)
+    const int *__restrict__ col_ncl;       // global column -> clusters
+    const float *__restrict__ overhang;    // per system, A
+    int n, n_pad, n_clusters;
+    float rc, rc2, rs2, sw_inv_den;
+    float beta;
+    float beta_p;        // A&S p * beta
+    float ewald_exp_c;   // beta^2 log2(e)
+    float ewald_fc;      // 2 beta / sqrt(pi)
+    int lj_on;
+    unsigned long long *f;
+    long long *energy;
+    int *status;
+    unsigned long long *stats;
+    int *dump;
+    long long dump_cap;
+    unsigned long long *dump_count;
+    const int *perm;
+    int split;        // work items (one warp each) per i-cluster
+    int persistent;   // 1: warps pull items from `queue` until none is left
+    int n_items;      // n_clusters * split
+    int *queue;       // next item (zeroed before each persistent launch)
+    int split_rings;  // 1: separate rings for LJ-carrying and charge-only j atoms
+};
+
+namespace {
+
+constexpr int kRing = 64;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Abramowitz & Stegun 7.1.26: erfc(x) ~ t(a1 + t(a2 + t(a3 + t(a4 + t a5)))) e^{-x^2},
+// t = 1/(1 + p x), |error| <= 1.5e-7
+constexpr float kAsP = 0.3275911f;
+constexpr float kAsA1 = 0.254829592f, kAsA2 = -0.284496736f, kAsA3 = 1.421413741f,
+                kAsA4 = -1.453152027f, kAsA5 = 1.061405429f;
+
+
+__device__ __forceinline__ void decode_shift(int code, const float (&L)[3], float &sx, float &sy,
+                                             float &sz) {
+    sx = (float)(code / 9 - 1) * L[0];
+    sy = (float)((code / 3) % 3 - 1) * L[1];
+    sz = (float)(code % 3 - 1) * L[2];
+}
+
+// One j entry staged in shared memory, two float4: the shifted coordinates
+// + charge, and (sigma/2, sqrt(4 eps), exclusion mask of the 32 i lanes,
+// cluster-order index) -- one 128-bit shared load each in the sweep.
+__device__ __forceinline__ void put_entry(float4 *ring, int pos, float4 xq, float2 prm,
+                                          unsigned mask, int jk) {
+    ring[2 * pos] = xq;
+    ring[2 * pos + 1] = make_float4(prm.x, prm.y, __uint_as_float(mask), __int_as_float(jk));
+}
+
+__device__ __forceinline__ void lds128(unsigned addr, float4 &v) {
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr));
+}
+
+// One work item: part `part` (of a.split) of i-cluster I's pair search.
+// HALF: the warp's two 16-lane halves sweep separate j lists, each holding
+// only the j atoms within rc of its own 16 i atoms' box.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool HALF>
+__device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int part,
+                                        float4 *s_j) {
+    // rings of 64 entries (2 float4 each): L = j atoms with LJ parameters,
+    // Q = charge-only j atoms; in HALF mode one pair of rings per half warp
+    float4 *const ringL = s_j, *const ringQ = s_j + 2 * kRing;
+    float4 *const ringL2 = s_j + 4 * kRing, *const ringQ2 = s_j + 6 * kRing;
+    const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
+    if (cI.w == 0.f) return;  // all-padding cluster
+    // this cluster's system: its box, and the range of clusters it may pair with
+    const int sid = a.cl_sys[I];
+    const SysDev &sd = a.sys[sid];
+    const float L[3] = {sd.L[0], sd.L[1], sd.L[2]};
+    const float invL[3] = {sd.invL[0], sd.invL[1], sd.invL[2]};
+    const int cl_lo = sd.cl_off, cl_hi = sd.cl_off + sd.cl_cap;
+    const int lane = threadIdx.x;
+    const unsigned lt = (1u << lane) - 1u;
+    const int ik = I * kCluster + lane;
+    const float4 xi = a.xq[ik];
+    const float2 pi = a.prm[ik];
+    const bool i_real = xi.x < 0.5f * kFarAway;
+    const int2 rI = a.prange[I];
+    const int ilo = I * kCluster;
+
+    float fix = 0.f, fiy = 0.f, fiz = 0.f;
+    double acc_lj = 0.0, acc_c = 0.0;  // per-lane energies: FP32 within a chunk, FP64 across
+    unsigned long long n_eval = 0, n_in = 0;
+    // two rings: j atoms with LJ parameters, and charge-only j atoms, whose
+    // sweeps skip the LJ arithmetic (two of every three water atoms)
+    int jbL = 0, jcL = 0, jbQ = 0, jcQ = 0;
+    int jbL2 = 0, jcL2 = 0, jbQ2 = 0, jcQ2 = 0;  // second half warp (HALF mode)
+
+    // Sweep of one 32-entry chunk starting at ring slot `base` (0 or 32).  At
+    // step t lane l pairs its i atom with entry l ^ t and keeps the i force;
+    // the j-force accumulator of entry e travels so that it always sits in
+    // the lane that pairs with e next (a butterfly shuffle with mask
+    // t ^ (t + 1)).  After step 31 lane l owns entry l ^ 31's complete j
+    // force.  The chunk is 1024-byte aligned, so entry l ^ t lives at
+    // (chunk | l << 5) ^ (t << 5): one logic op per step for the address.
+    const unsigned lanebit = 1u << lane;
+    auto chunk = [&](auto with_lj, auto width, unsigned sa) {
+        constexpr bool WL = decltype(with_lj)::value;
+        constexpr int W = decltype(width)::value;  // 32: whole warp; 16: per half warp
+        const int li = lane & (W - 1);
+        float fjx = 0.f, fjy = 0.f, fjz = 0.f;
+        float c_lj = 0.f, c_c = 0.f;
+        auto step = [&](const float4 &xj, const float4 &aux, unsigned shfl_mask) {
+            const unsigned mk = __float_as_uint(aux.z);
+            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            // masked and out-of-range pairs may compute inf/NaN (r2 = 0 for an
+            // atom with itself); every use below selects them away
+            const bool inc = (r2 <= a.rc2) && !(mk & lanebit);
+            if (DUMP && inc) {
+                unsigned long long slot = atomicAdd(a.dump_count, 1ull);
+                if ((long long)slot < a.dump_cap) {
+                    int pj_atom = a.perm[__float_as_int(aux.w)], pi_atom = a.perm[ik];
+                    a.dump[2 * slot] = min(pi_atom, pj_atom);
+                    a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
+                }
+            }
+            const float rinv = rsqrtf(r2);
+            const float rinv2 = rinv * rinv;
+            float fr = 0.f, elj = 0.f, ecl = 0.f;
+            if (LJ && WL) {
+                const float sig = pi.x + aux.x;
+                const float s2 = sig * sig * rinv2;
+                const float s6 = s2 * s2 * s2;
+                const float c6 = pi.y * aux.y * s6;
+                float flj = c6 * fmaf(12.0f, s6, -6.0f) * rinv2;
+                if (SWITCH) {
+                    // CHARMM switch, branch free: below rs the clamped r^2 gives
+                    // sw = 1 and dsw = 0 exactly
+                    elj = c6 * (s6 - 1.0f);
+                    const float r2c = fmaxf(r2, a.rs2);
+                    const float u = a.rc2 - r2c;
+                    const float sw = u * u * fmaf(2.0f, r2c, a.rc2 - 3.0f * a.rs2) * a.sw_inv_den;
+                    const float dsw = 12.0f * u * (a.rs2 - r2c) * a.sw_inv_den;
+                    flj = fmaf(flj, sw, -elj * dsw);
+                    elj *= sw;
+                } else if (ENERGY) {
+                    elj = c6 * (s6 - 1.0f);
+                }
+                fr = flj;
+            }
+            if (COUL == MDG_COUL_EWALD) {
+                const float qq = xi.w * xj.w;
+                const float r = r2 * rinv;
+                const float tt = __fdividef(1.0f, fmaf(a.beta_p, r, 1.0f));
+                const float poly =
+                    tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, kAsA5, kAsA4), kAsA3), kAsA2), kAsA1);
+                const float ex = exp2f(-a.ewald_exp_c * r2);
+                const float ecf = qq * poly * ex * rinv;
+                fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecf), rinv2, fr);
+                // the force keeps the 1.5e-7 approximation in every variant (so a
+                // trajectory does not depend on when energies are reported); the
+                // reported energy uses the library erfc, whose error does not pile
+                // up over 10^6 pairs
+                if (ENERGY) ecl = qq * erfcf(a.beta * r) * rinv;
+            }
+            fr = inc ? fr : 0.f;
+            fix = fmaf(-fr, dx, fix);
+            fiy = fmaf(-fr, dy, fiy);
+            fiz = fmaf(-fr, dz, fiz);
+            fjx = fmaf(fr, dx, fjx);
+            fjy = fmaf(fr, dy, fjy);
+            fjz = fmaf(fr, dz, fjz);
+            if (ENERGY) {
+                c_lj += inc ? elj : 0.f;
+                c_c += inc ? ecl : 0.f;
+                n_in += __popc(__ballot_sync(kFull, inc));
+            }
+            fjx = __shfl_xor_sync(kFull, fjx, shfl_mask);
+            fjy = __shfl_xor_sync(kFull, fjy, shfl_mask);
+            fjz = __shfl_xor_sync(kFull, fjz, shfl_mask);
+        };
+        // each step's entry is loaded one step ahead, so its shared-memory
+        // latency overlaps the previous step's arithmetic
+        float4 xa, aa, xb, ab;
+        lds128(sa | ((unsigned)li << 5), xa);
+        lds128((sa | ((unsigned)li << 5)) + 16u, aa);
+#pragma unroll 1
+        for (int t0 = 0; t0 < W; t0 += 4) {
+            const unsigned sb = sa | ((unsigned)(li ^ t0) << 5);
+            // masks t ^ (t + 1) for t = t0 .. t0 + 3 (below W: a half warp's
+            // accumulators stay in that half); none after the last step
+            const unsigned m3 = t0 == W - 4 ? 0u : (unsigned)((t0 + 3) ^ (t0 + 4));
+            lds128(sb ^ 32u, xb);
+            lds128((sb ^ 32u) + 16u, ab);
+            step(xa, aa, 1u);
+            lds128(sb ^ 64u, xa);
+            lds128((sb ^ 64u) + 16u, aa);
+            step(xb, ab, 3u);
+            lds128(sb ^ 96u, xb);
+            lds128((sb ^ 96u) + 16u, ab);
+            step(xa, aa, 1u);
+            if (t0 < W - 4) {
+                const unsigned nb = sa | ((unsigned)(li ^ (t0 + 4)) << 5);
+                lds128(nb, xa);
+                lds128(nb + 16u, aa);
+            }
+            step(xb, ab, m3);
+        }
+        float4 own;
+        lds128(sa + ((unsigned)(li ^ (W - 1)) << 5) + 16u, own);
+        const int jk = __float_as_int(own.w);
+        if (jk >= 0 && !DUMP) {
+            if (!(fabsf(fjx) < kFixLimit && fabsf(fjy) < kFixLimit && fabsf(fjz) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            fix_red(&a.f[jk], to_fix(fjx));
+            fix_red(&a.f[a.n_pad + jk], to_fix(fjy));
+            fix_red(&a.f[2 * a.n_pad + jk], to_fix(fjz));
+        }
+        if (ENERGY) {
+            acc_lj += (double)c_lj;
+            acc_c += (double)c_c;
+        }
+        n_eval += W * 32;
+        __syncwarp();
+    };
+    auto shared_addr = [](const float4 *p) { return (unsigned)__cvta_generic_to_shared(p); };
+
+    // HALF mode: one 16-step sweep of up to 16 entries of each half's ring of
+    // one kind; a half with fewer pending entries is padded with far-away ones
+    auto sweep16 = [&](auto with_lj) {
+        constexpr bool WL = decltype(with_lj)::value;
+        int &cA = WL ? jcL : jcQ, &bA = WL ? jbL : jbQ;
+        int &cB = WL ? jcL2 : jcQ2, &bB = WL ? jbL2 : jbQ2;
+        float4 *const rA = WL ? ringL : ringQ, *const rB = WL ? ringL2 : ringQ2;
+        const int h = lane >> 4, li = lane & 15;
+        const int c = h ? cB : cA, b = h ? bB : bA;
+        float4 *const r = h ? rB : rA;
+        if (li >= c)
+            put_entry(r, (b + li) & (kRing - 1), make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                      make_float2(0.f, 0.f), kFull, -1);
+        __syncwarp();
+        chunk(with_lj, std::integral_constant<int, 16>{}, shared_addr(r + 2 * b));
+        cA -= min(16, cA);
+        bA = (bA + 16) & (kRing - 1);
+        cB -= min(16, cB);
+        bB = (bB + 16) & (kRing - 1);
+    };
+
+    // one candidate (J, image) found by the scan: test J's atoms against I's box
+    // and append the survivors to this warp's ring (chunk sweeps when full)
+    auto candidate = [&](int J, int code) {
+        float sx, sy, sz;
+        decode_shift(code, L, sx, sy, sz);
+        const int jk = J * kCluster + lane;
+        float4 xj = a.xq[jk];
+        xj.x += sx;
+        xj.y += sy;
+        xj.z += sz;
+        // exclusion mask of the i lanes for this j atom
+        auto excl_mask = [&]() {
+            unsigned m = 0u;
+            if (J == I) m = kFull << lane;  // half shell inside the cluster
+            if (rI.y >= J * kCluster && rI.x < (J + 1) * kCluster) {
+                for (int w = 0; w < a.pw; ++w) {
+                    const int p = a.partners[(size_t)jk * a.pw + w];
+                    if (p >= 0) {
+                        const int pk = (p & 0x3fffffff) - ilo;
+                        if (pk >= 0 && pk < kCluster) m |= 1u << pk;
+                    }
+                }
+            }
+            return m;
+        };
+        if constexpr (HALF) {
+            auto box_hit = [&](const float4 c, const float4 h) {
+                const float ux = fmaxf(fabsf(xj.x - c.x) - h.x, 0.f);
+                const float uy = fmaxf(fabsf(xj.y - c.y) - h.y, 0.f);
+                const float uz = fmaxf(fabsf(xj.z - c.z) - h.z, 0.f);
+                return fmaf(ux, ux, fmaf(uy, uy, uz * uz)) <= a.rc2;
+            };
+            // a half with no atoms has a far-away box, which far-away padding
+            // j slots would "hit": its w (1 when the half has atoms) gates it
+            const float4 cA = a.hbox[4 * I], cB = a.hbox[4 * I + 2];
+            const bool hitA = cA.w > 0.f && box_hit(cA, a.hbox[4 * I + 1]);
+            const bool hitB = cB.w > 0.f && box_hit(cB, a.hbox[4 * I + 3]);
+            const float2 pj = (hitA || hitB) ? a.prm[jk] : make_float2(0.f, 0.f);
+            const bool to_l = !a.split_rings || (LJ && pj.y != 0.f);
+            const bool keep_q = COUL == MDG_COUL_EWALD || DUMP;
+            const bool aL = hitA && to_l, aQ = hitA && !to_l && keep_q;
+            const bool bL = hitB && to_l, bQ = hitB && !to_l && keep_q;
+            const unsigned mAL = __ballot_sync(kFull, aL), mAQ = __ballot_sync(kFull, aQ);
+            const unsigned mBL = __ballot_sync(kFull, bL), mBQ = __ballot_sync(kFull, bQ);
+            if ((mAL | mAQ | mBL | mBQ) == 0u) return;
+            if (aL || aQ || bL || bQ) {
+                const unsigned m = excl_mask();
+                if (aL) put_entry(ringL, (jbL + jcL + __popc(mAL & lt)) & (kRing - 1), xj, pj, m, jk);
+                if (aQ) put_entry(ringQ, (jbQ + jcQ + __popc(mAQ & lt)) & (kRing - 1), xj, pj, m, jk);
+                if (bL) put_entry(ringL2, (jbL2 + jcL2 + __popc(mBL & lt)) & (kRing - 1), xj, pj, m, jk);
+                if (bQ) put_entry(ringQ2, (jbQ2 + jcQ2 + __popc(mBQ & lt)) & (kRing - 1), xj, pj, m, jk);
+            }
+            jcL += __popc(mAL);
+            jcQ += __popc(mAQ);
+            jcL2 += __popc(mBL);
+            jcQ2 += __popc(mBQ);
+            __syncwarp();
+            // every ring stays below 32 pending entries between candidates
+            while (jcL >= 32 || jcL2 >= 32 || (jcL >= 16 && jcL2 >= 16)) sweep16(std::true_type{});
+            while (jcQ >= 32 || jcQ2 >= 32 || (jcQ >= 16 && jcQ2 >= 16)) sweep16(std::false_type{});
+            return;
+        }
+        const float gx = fmaxf(fabsf(xj.x - cI.x) - hI.x, 0.f);
+        const float gy = fmaxf(fabsf(xj.y - cI.y) - hI.y, 0.f);
+        const float gz = fmaxf(fabsf(xj.z - cI.z) - hI.z, 0.f);
+        const bool hit = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) <= a.rc2;
+        const float2 pj = hit ? a.prm[jk] : make_float2(0.f, 0.f);
+        // With split rings, LJ-carrying atoms go to ring L and the rest,
+        // which matter only for the Ewald term (or the pair-set dump), to
+        // ring Q; otherwise every hit goes to ring L.
+        const bool to_l = !a.split_rings || (LJ && pj.y != 0.f);
+        const bool hitL = hit && to_l;
+        const bool hitQ = hit && !to_l && (COUL == MDG_COUL_EWALD || DUMP);
+        const unsigned bL = __ballot_sync(kFull, hitL), bQ = __ballot_sync(kFull, hitQ);
+        if ((bL | bQ) == 0u) return;
+        if (hitL || hitQ) {
+            const unsigned m = excl_mask();
+            if (hitL) put_entry(ringL, (jbL + jcL + __popc(bL & lt)) & (kRing - 1), xj, pj, m, jk);
+            else put_entry(ringQ, (jbQ + jcQ + __popc(bQ & lt)) & (kRing - 1), xj, pj, m, jk);
+        }
+        jcL += __popc(bL);
+        jcQ += __popc(bQ);
+        __syncwarp();
+        if (jcL >= 32) {
+            chunk(std::true_type{}, std::integral_constant<int, 32>{}, shared_addr(ringL + 2 * jbL));
+            jbL = (jbL + 32) & (kRing - 1);
+            jcL -= 32;
+        }
+        if (jcQ >= 32) {
+            chunk(std::false_type{}, std::integral_constant<int, 32>{}, shared_addr(ringQ + 2 * jbQ));
+            jbQ = (jbQ + 32) & (kRing - 1);
+            jcQ -= 32;
+        }
+    };
+
+    // Candidate clusters.  Work item `part` scans batches part, part + split,
+    // ... of 32 clusters, so the split warps of one i-cluster share its
+    // neighbourhood without talking to each other.
+    // Balanced half shell: the cluster pair {I, J} (I != J) belongs to I when
+    // I < J and I + J is odd, or when I > J and I + J is even -- every cluster
+    // owns about half of its neighbours whatever its index; J == I is kept and
+    // split by the lane mask.  Periodic images: the nearest image of J's box
+    // centre, or all 27 when a box pair spans half the box.
+    unsigned n_cand = 0;
+    // every lane offers one (J, image) candidate; the hits go to candidate()
+    auto offer = [&](bool hit, int J, int code) {
+        unsigned b = __ballot_sync(kFull, hit);
+        if (ENERGY) n_cand += __popc(b);
+        while (b) {
+            const int src = __ffs(b) - 1;
+            b &= b - 1;
+            candidate(__shfl_sync(kFull, J, src), __shfl_sync(kFull, code, src));
+        }
+    };
+    // the half-shell owner rule
+    auto owned = [&](int J) { return J == I || ((I + J) & 1) == (I < J ? 1 : 0); };
+
+    // Column mode (systems whose columns span at least 2R+1 in x and y):
+    // candidates come only from the (2R+1)^2 columns around I's column, R =
+    // the column reach of rc plus twice the largest distance any cluster box
+    // has moved out of its column since the last re-sort.  Each column is a
+    // contiguous run of clusters; the runs are concatenated into one virtual
+    // list (warp scan of the run lengths) walked 32 at a time.
+    int R = 0;
+    bool colmode = sd.col_mode != 0;
+    if (colmode) {
+        const float ov = a.overhang[sid];
+        const float aw = fminf(L[0] / (float)sd.ncx, L[1] / (float)sd.ncy);
+        R = (int)floorf((a.rc + 2.f * ov) / aw) + 1;
+        colmode = 2 * R + 1 <= min(sd.ncx, sd.ncy);
+    }
+    if (colmode) {
+        const int pk = a.col_xy[a.cl_col[I]];
+        const int cx = pk >> 16, cy = pk & 0xffff;
+        const int side = 2 * R + 1, ncn = side * side;
+        const int base0 = a.col_cl_start[sd.col_off];
+        for (int cb = 0; cb < ncn; cb += 32) {
+            const int c = cb + lane;
+            int cnt = 0, start = 0, shc = 4;  // shc: (sx + 1) * 3 + (sy + 1)
+            if (c < ncn) {
+                int x2 = cx + c / side - R, y2 = cy + c % side - R;
+                const int sx = x2 < 0 ? -1 : (x2 >= sd.ncx ? 1 : 0);
+                const int sy = y2 < 0 ? -1 : (y2 >= sd.ncy ? 1 : 0);
+                x2 -= sx * sd.ncx;
+                y2 -= sy * sd.ncy;
+                const int gc = sd.col_off + a.col_rank[sd.col_off + x2 * sd.ncy + y2];
+                start = sd.cl_off + a.col_cl_start[gc] - base0;
+                cnt = a.col_ncl[gc];
+                shc = (sx + 1) * 3 + (sy + 1);
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(kFull, incl, 31);
+            for (int v0 = part * 32; v0 < total; v0 += a.split * 32) {
+                const int v = v0 + lane;
+                int lo = 0, hi = 31;  // first lane whose inclusive count exceeds v
+#pragma unroll
+                for (int it = 0; it < 5; ++it) {
+                    const int mid = (lo + hi) >> 1;
+                    const int im = __shfl_sync(kFull, incl, mid);
+                    if (im > v) hi = mid;
+                    else lo = mid + 1;
+                }
+                const int s_incl = __shfl_sync(kFull, incl, lo);
+                const int s_cnt = __shfl_sync(kFull, cnt, lo);
+                const int s_start = __shfl_sync(kFull, start, lo);
+                const int s_shc = __shfl_sync(kFull, shc, lo);
+                const int J = s_start + (v - (s_incl - s_cnt));
+                bool valid = v < total && owned(J);
+                float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                       hJ = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (valid) {
+                    cJ = a.bbox[2 * J];
+                    hJ = a.bbox[2 * J + 1];
+                }
+                valid = valid && cJ.w > 0.f;
+                // x and y images follow from the column wrap; z takes the
+                // nearest image of the box centres, or all three when a box
+                // pair spans half the box height
+                const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+                const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+                const float gx = fmaxf(fabsf(fmaf((float)(s_shc / 3 - 1), L[0], d[0])) - h[0], 0.f);
+                const float gy = fmaxf(fabsf(fmaf((float)(s_shc % 3 - 1), L[1], d[1])) - h[1], 0.f);
+                const float gxy = fmaf(gx, gx, gy * gy);
+                float nz = -rintf(d[2] * invL[2]);
+                nz = fminf(fmaxf(nz, -1.f), 1.f);
+                const float gz = fmaxf(fabsf(fmaf(nz, L[2], d[2])) - h[2], 0.f);
+                const bool near_hit = valid && fmaf(gz, gz, gxy) <= a.rc2;
+                const bool multi_z = valid && (h[2] + a.rc >= 0.5f * L[2]);
+                if (!__any_sync(kFull, multi_z)) {
+                    offer(near_hit, J, s_shc * 3 + (int)nz + 1);
+                } else {
+                    for (int zz = -1; zz <= 1; ++zz) {
+                        bool hit = near_hit && zz == (int)nz;
+                        if (multi_z) {
+                            const float g = fmaxf(fabsf(fmaf((float)zz, L[2], d[2])) - h[2], 0.f);
+                            hit = fmaf(g, g, gxy) <= a.rc2;
+                        }
+                        offer(hit, J, s_shc * 3 + zz + 1);
+                    }
+                }
+            }
+        }
+    } else {
+        // full scan of the system's clusters: work item `part` takes batches
+        // part, part + split, ... of 32 clusters
+        for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += a.split * 32) {
+            const int J = J0 + lane;
+            bool valid = J < cl_hi && owned(J);
+            float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                   hJ = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) {
+                cJ = a.bbox[2 * J];
+                hJ = a.bbox[2 * J + 1];
+            }
+            const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+            const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+            int ncode = 0;
+            float g2 = 0.f;
+            bool multi = false;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float nk = -rintf(d[k] * invL[k]);
+                nk = fminf(fmaxf(nk, -1.f), 1.f);
+                const float dd = fmaf(nk, L[k], d[k]);
+                const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                g2 = fmaf(gap, gap, g2);
+                ncode = ncode * 3 + (int)nk + 1;
+                multi = multi || (h[k] + a.rc >= 0.5f * L[k]);
+            }
+            valid = valid && cJ.w > 0.f;
+            multi = multi && valid;
+            const bool near_hit = valid && g2 <= a.rc2;
+            if (!__any_sync(kFull, multi)) {
+                offer(near_hit, J, ncode);
+            } else {
+                for (int code = 0; code < 27; ++code) {
+                    bool hit = near_hit && code == ncode;
+                    if (multi) {
+                        const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
+                        float gg = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            const float dd = fmaf((float)s3[k], L[k], d[k]);
+                            const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                            gg = fmaf(gap, gap, gg);
+                        }
+                        hit = gg <= a.rc2;
+                    }
+                    offer(hit, J, code);
+                }
+            }
+        }
+    }
+    // The partial last chunks, padded with far-away entries.  When both fit
+    // in one chunk the charge-only entries join the LJ chunk (their LJ terms
+    // are zero), so an item ends with at most one partial sweep.
+    if constexpr (HALF) {
+        if ((jcQ > 0 || jcQ2 > 0) && jcL + jcQ <= 16 && jcL2 + jcQ2 <= 16) {
+            const int h = lane >> 4, li = lane & 15;
+            const int cq = h ? jcQ2 : jcQ;
+            if (li < cq) {
+                const float4 *src = (h ? ringQ2 : ringQ) + 2 * (((h ? jbQ2 : jbQ) + li) & (kRing - 1));
+                float4 *dst = (h ? ringL2 : ringL) +
+                              2 * (((h ? jbL2 : jbL) + (h ? jcL2 : jcL) + li) & (kRing - 1));
+                const float4 e0 = src[0], e1 = src[1];
+                dst[0] = e0;
+                dst[1] = e1;
+            }
+            jcL += jcQ;
+            jcQ = 0;
+            jcL2 += jcQ2;
+            jcQ2 = 0;
+            __syncwarp();
+        }
+        while (jcL > 0 || jcL2 > 0) sweep16(std::true_type{});
+        while (jcQ > 0 || jcQ2 > 0) sweep16(std::false_type{});
+    }
+    if (!HALF && jcQ > 0 && jcL + jcQ <= 32) {
+        if (lane < jcQ) {
+            const float4 *src = ringQ + 2 * ((jbQ + lane) & (kRing - 1));
+            float4 *dst = ringL + 2 * ((jbL + jcL + lane) & (kRing - 1));
+            const float4 e0 = src[0], e1 = src[1];
+            dst[0] = e0;
+            dst[1] = e1;
+        }
+        jcL += jcQ;
+        jcQ = 0;
+        __syncwarp();
+    }
+    if (!HALF && jcL > 0) {
+        if (lane >= jcL)
+            put_entry(ringL, (jbL + lane) & (kRing - 1), make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                      make_float2(0.f, 0.f), kFull, -1);
+        __syncwarp();
+        chunk(std::true_type{}, std::integral_constant<int, 32>{}, shared_addr(ringL + 2 * jbL));
+    }
+    if (!HALF && jcQ > 0) {
+        if (lane >= jcQ)
+            put_entry(ringQ, (jbQ + lane) & (kRing - 1), make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                      make_float2(0.f, 0.f), kFull, -1);
+        __syncwarp();
+        chunk(std::false_type{}, std::integral_constant<int, 32>{}, shared_addr(ringQ + 2 * jbQ));
+    }
+
+    // ---- this work item's share of the i forces and energies -------------
+    if (!DUMP && i_real) {
+        if (!(fabsf(fix) < kFixLimit && fabsf(fiy) < kFixLimit && fabsf(fiz) < kFixLimit))
+            raise_status(a.status, MDG_ERR_OVERFLOW);
+        fix_red(&a.f[ik], to_fix(fix));
+        fix_red(&a.f[a.n_pad + ik], to_fix(fiy));
+        fix_red(&a.f[2 * a.n_pad + ik], to_fix(fiz));
+    }
+    if (ENERGY) {
+        const double el = warp_sum_d(acc_lj), ee = warp_sum_d(acc_c);
+        if (lane == 0) {
+            if (!(fabs(el) < kFixLimit && fabs(ee) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            long long *es = a.energy + sid * kEnergySlots;
+            fix_red((unsigned long long *)&es[MDG_TERM_LJ], to_fix_d(el));
+            fix_red((unsigned long long *)&es[MDG_TERM_COUL_REAL], to_fix_d(ee));
+            atomicAdd(&a.stats[0], n_eval);
+            atomicAdd(&a.stats[1], n_in);
+            atomicAdd(&a.stats[2], (unsigned long long)n_cand);
+            if (part == 0) atomicAdd(&a.stats[3], 1ull);
+        }
+    }
+}
+
+// Grid form: one one-warp CTA per work item, scheduled by the hardware.
+// Persistent form: enough warps to fill the GPU once, each pulling work
+// items from a device counter until none is left.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool HALF>
+__global__ void __launch_bounds__(32, ENERGY ? 16 : 20) k_nonbonded(NbArgs a) {
+    // two rings of 64 entries of 32 bytes; each 32-entry chunk starts on a
+    // 1024-byte boundary
+    __shared__ __align__(1024) float4 s_j[(HALF ? 8 : 4) * kRing];
+    if (!a.persistent) {
+        nb_item<COUL, LJ, SWITCH, ENERGY, DUMP, HALF>(a, blockIdx.x / a.split, blockIdx.x % a.split,
+                                                s_j);
+        return;
+    }
+    for (;;) {
+        int item = 0;
+        if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
+        item = __shfl_sync(kFull, item, 0);
+        if (item >= a.n_items) break;
+        __syncwarp();  // the previous item's ring reads are done
+        nb_item<COUL, LJ, SWITCH, ENERGY, DUMP, HALF>(a, item / a.split, item % a.split, s_j);
+    }
+}
+
+template <int COUL, bool LJ, bool SW, bool HALF>
+cudaError_t dispatch_nb(mdg_system *s, const NbArgs &a, int energy, int dump) {
+    dim3 grid(a.persistent ? s->nb_persistent_ctas : a.n_items), block(32);
+    if (a.persistent && cudaMemsetAsync(a.queue, 0, sizeof(int), s->stream) != cudaSuccess)
+        return cudaGetLastError();
+    if (dump)
+        k_nonbonded<COUL, LJ, SW, false, true, HALF><<<grid, block, 0, s->stream>>>(a);
+    else if (energy)
+        k_nonbonded<COUL, LJ, SW, true, false, HALF><<<grid, block, 0, s->stream>>>(a);
+    else
+        k_nonbonded<COUL, LJ, SW, false, false, HALF><<<grid, block, 0, s->stream>>>(a);
+    return cudaGetLastError();
+}
+
+// every (Coulomb, LJ, switch) combination the library launches, for one HALF
+template <bool HALF>
+cudaError_t dispatch_shape(mdg_system *s, const NbArgs &a, int coul_tile, bool want_lj, bool sw,
+                           int energy, int dump) {
+    if (coul_tile == MDG_COUL_EWALD && !want_lj)
+        return dispatch_nb<MDG_COUL_EWALD, false, false, HALF>(s, a, energy, dump);
+    if (coul_tile == MDG_COUL_EWALD)
+        return sw ? dispatch_nb<MDG_COUL_EWALD, true, true, HALF>(s, a, energy, dump)
+                  : dispatch_nb<MDG_COUL_EWALD, true, false, HALF>(s, a, energy, dump);
+    return sw ? dispatch_nb<MDG_COUL_NONE, true, true, HALF>(s, a, energy, dump)
+              : dispatch_nb<MDG_COUL_NONE, true, false, HALF>(s, a, energy, dump);
+}
+
+}  // namespace
+}  // namespace mdg

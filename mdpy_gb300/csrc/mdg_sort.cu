@@ -257,79 +257,15 @@ __global__ void k_partners_sorted(const int *__restrict__ perm, const int *__res
 
 // one warp per cluster: FP32 coordinates + scaled charge, bounding box, and
 // zeroing of the cluster's fixed-point force slots for the coming evaluation
-__global__ void k_pack(const double *__restrict__ x, const int *__restrict__ perm,
-                       const float *__restrict__ q_sorted, int n_clusters, int n_pad,
-                       float4 *__restrict__ xq, float4 *__restrict__ bbox,
-                       unsigned long long *__restrict__ f, const SysDev *__restrict__ sys,
-                       const int *__restrict__ cl_sys, const int *__restrict__ cl_col,
-                       const int *__restrict__ col_xy, float *__restrict__ overhang) {
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (warp >= n_clusters) return;
-    int k = warp * kCluster + lane;
-    int i = perm[k];
-    float4 p;
-    bool valid = i >= 0;
-    if (valid) {
-        // Between re-sorts the FP64 positions drift freely out of [0, L).
-        // The pair search tries the images -1, 0, +1 of each cluster pair,
-        // which is exact while every stored coordinate stays within a window
-        // of width 1.5 L: a coordinate that leaves [-L/4, 5L/4) is wrapped
-        // back into [0, L) here (its cluster box then spans the box, and the
-        // search covers it with all 27 images).
-        const double *Ld = sys[cl_sys[warp]].Ld;
-        double c[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            c[d] = x[3 * i + d];
-            if (c[d] < -0.25 * Ld[d] || c[d] >= 1.25 * Ld[d]) c[d] -= Ld[d] * floor(c[d] / Ld[d]);
-        }
-        p = make_float4((float)c[0], (float)c[1], (float)c[2], q_sorted[k]);
-    } else {
-        p = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
-    }
-    xq[k] = p;
-    f[k] = 0ull;
-    f[n_pad + k] = 0ull;
-    f[2 * n_pad + k] = 0ull;
-    float lox = valid ? p.x : INFINITY, loy = valid ? p.y : INFINITY, loz = valid ? p.z : INFINITY;
-    float hix = valid ? p.x : -INFINITY, hiy = valid ? p.y : -INFINITY,
-          hiz = valid ? p.z : -INFINITY;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
-        loy = fminf(loy, __shfl_xor_sync(0xffffffffu, loy, o));
-        loz = fminf(loz, __shfl_xor_sync(0xffffffffu, loz, o));
-        hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
-        hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
-        hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
-    }
-    int cnt = __popc(__ballot_sync(0xffffffffu, valid));
-    if (lane == 0) {
-        if (cnt == 0) {  // an all-padding cluster: far away, zero extent
-            bbox[2 * warp] = make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
-            bbox[2 * warp + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        } else {
-            bbox[2 * warp] = make_float4(0.5f * (lox + hix), 0.5f * (loy + hiy),
-                                         0.5f * (loz + hiz), (float)cnt);
-            bbox[2 * warp + 1] = make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy),
-                                             0.5f * (hiz - loz), 0.0f);
-            // how far the box reaches out of its sort column in x and y
-            const int c = cl_col[warp];
-            if (c >= 0) {
-                const int q = cl_sys[warp];
-                const SysDev &d = sys[q];
-                const int pk = col_xy[c];
-                const float ax = d.L[0] / (float)d.ncx, ay = d.L[1] / (float)d.ncy;
-                const float x0 = (float)(pk >> 16) * ax, y0 = (float)(pk & 0xffff) * ay;
-                const float ov = fmaxf(fmaxf(fmaxf(x0 - lox, hix - (x0 + ax)),
-                                             fmaxf(y0 - loy, hiy - (y0 + ay))),
-                                       0.0f);
-                if (ov > overhang[q])
-                    atomicMax((unsigned int *)&overhang[q], __float_as_uint(ov));
-            }
-        }
-    }
+__global__ void k_pack(PackArgs a) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= a.n_clusters) return;
+    const int k = warp * kCluster + (threadIdx.x & 31);
+    const int i = a.perm[k];
+    double c[3] = {0.0, 0.0, 0.0};
+    if (i >= 0)
+        for (int d = 0; d < 3; ++d) c[d] = a.x[3 * i + d];
+    pack_cluster(a, warp, k, i >= 0, c);
 }
 
 inline unsigned spread2(unsigned v) {
@@ -414,6 +350,7 @@ int prepare_sort_grid(mdg_system *s) {
             (rc = realloc_dev(&s->prm_sorted, n_pad)) || (rc = realloc_dev(&s->xq, n_pad)) ||
             (rc = realloc_dev(&s->f, 3 * (size_t)n_pad)) ||
             (rc = realloc_dev(&s->bbox, 2 * (size_t)n_clusters)) ||
+            (rc = realloc_dev(&s->hbox, 4 * (size_t)n_clusters)) ||
             (rc = realloc_dev(&s->cluster_partner_range, n_clusters)) ||
             (rc = realloc_dev(&s->cl_sys, n_clusters)) ||
             (rc = realloc_dev(&s->cl_col, n_clusters)) ||
@@ -482,11 +419,28 @@ cudaError_t launch_reorder(mdg_system *s) {
     return cudaGetLastError();
 }
 
+PackArgs make_pack_args(mdg_system *s) {
+    PackArgs a;
+    a.x = s->x;
+    a.perm = s->perm;
+    a.q_sorted = s->q_sorted;
+    a.n_clusters = s->n_clusters;
+    a.n_pad = s->n_pad;
+    a.xq = s->xq;
+    a.bbox = s->bbox;
+    a.hbox = s->hbox;
+    a.f = s->f;
+    a.sys = s->sys_dev;
+    a.cl_sys = s->cl_sys;
+    a.cl_col = s->cl_col;
+    a.col_xy = s->col_xy;
+    a.overhang = s->overhang;
+    return a;
+}
+
 cudaError_t launch_pack(mdg_system *s) {
     const int tb = 256;
-    k_pack<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, s->stream>>>(
-        s->x, s->perm, s->q_sorted, s->n_clusters, s->n_pad, s->xq, s->bbox, s->f, s->sys_dev,
-        s->cl_sys, s->cl_col, s->col_xy, s->overhang);
+    k_pack<<<(s->n_clusters * 32 + tb - 1) / tb, tb, 0, s->stream>>>(make_pack_args(s));
     s->launches += 1;
     return cudaGetLastError();
 }

@@ -144,3 +144,37 @@ def test_simulation_with_log_dumper(lib, tmp_path):
     # the lattice start relaxes: temperatures move, but stay finite and positive
     assert all(np.isfinite(t) and t > 0 for t in temps)
     assert float(log.rows[-1][5]) > 0   # ns/day column
+
+
+def test_charmm_forcefield_ensemble_runs_on_the_device(lib):
+    """An mdpy-style script: CharmmForcefield -> create_ensemble -> update ->
+    Simulation.integrate, with PME as the long-range solver; the forces equal
+    those of the same constraints added by hand."""
+    from mdpy_gb300 import constraint as C, systems
+    from mdpy_gb300.ensemble import Ensemble
+    from mdpy_gb300.forcefield import CharmmForcefield
+    from mdpy_gb300.integrator import LangevinIntegrator
+    from mdpy_gb300.simulation import LogDumper, Simulation
+
+    w = systems.water_box(500, 25.0, seed=4)
+    ff = CharmmForcefield(w.topology, w.pbc_matrix, cutoff_radius=10.0, long_range_solver="PME",
+                          ewald_error=1e-5, pme_grid_spacing=1.0)
+    ff.set_parameters(w.parameters)
+    ens = ff.create_ensemble()
+    ens.state.set_positions(w.positions)
+    ens.update()
+    ref = Ensemble(w.topology, w.pbc_matrix)
+    ref.add_constraints(C.NonbondedConstraint(w.parameters["nonbonded"], 10.0, ewald_error=1e-5),
+                        C.PMEConstraint(ewald_error=1e-5, real_space_cutoff=10.0,
+                                        grid_spacing=1.0),
+                        C.CharmmBondConstraint(w.parameters["bond"]),
+                        C.CharmmAngleConstraint(w.parameters["angle"]))
+    ref.state.set_positions(w.positions)
+    ref.update()
+    assert np.array_equal(ens.forces, ref.forces)
+    assert ens.potential_energy == ref.potential_energy
+    ens.state.set_velocities_to_temperature(300, seed=1)
+    sim = Simulation(ens, LangevinIntegrator(1.0, 300.0, 0.001, seed=2))
+    sim.add_dumpers(LogDumper(None, dump_frequency=10))
+    sim.integrate(20)
+    assert np.isfinite(ens.potential_energy) and ens.kinetic_energy > 0

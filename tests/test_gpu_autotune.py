@@ -31,20 +31,20 @@ def test_every_shape_gives_the_same_forces(lib, orc, edge, n_waters):
     ref_pairs = None
     ref_f = None
     for split in (1, 2, 4, 8, 16):
-        for persistent in (0, 20):
+        for persistent, half in ((0, 0), (20, 0), (0, 1), (20, 1)):
             s.set_launch_shape(split, persistent, (64, 128, 256)[split % 3], split % 2,
-                               (split // 2) % 2, split % 4)
+                               (split // 2) % 2, split % 4, half)
             pairs = pairs_to_set(s.pairset())
             s.compute_forces(mask)
             f1 = s.get_forces()
             s.compute_forces(mask)
             f2 = s.get_forces()
-            assert np.array_equal(f1, f2), (split, persistent)     # reproducible
+            assert np.array_equal(f1, f2), (split, persistent, half)     # reproducible
             if ref_f is None:
                 ref_pairs, ref_f = pairs, f1
             else:
-                assert pairs == ref_pairs
-                assert rel_rms(f1, ref_f) < 1e-6, (split, persistent)
+                assert pairs == ref_pairs, (split, persistent, half)
+                assert rel_rms(f1, ref_f) < 1e-6, (split, persistent, half)
     with pytest.raises(Exception, match="split"):
         s.set_launch_shape(3, 0, 256)
     with pytest.raises(Exception, match="PME block"):
@@ -67,6 +67,7 @@ def test_autotune_keeps_a_valid_shape(lib, orc):
     assert r["split"] in (2, 4, 8) and r["pme_block"] in (64, 128, 256)
     assert r["persistent"] in (0, 20, 24) and r["side_priority"] in (0, 1)
     assert r["split_rings"] in (0, 1) and r["pme_tiles"] in (0, 1, 2, 3) and r["tuned_ms"] > 0
+    assert r["half"] in (0, 1)
     with pytest.raises(Exception, match="no force evaluation"):
         s.get_forces()
     s.compute_forces(mask)
@@ -97,7 +98,7 @@ def test_autotune_over_md_steps_restores_the_state(lib, orc):
         if tune:
             r = s.autotune(mask, reps=2)
             assert r["tuned_ms"] > 0
-            s.set_launch_shape(4, 0, 256, 0, 1, 0)  # compare under one shape
+            s.set_launch_shape(4, 0, 256, 0, 1, 0, 0)  # compare under one shape
         s.integrate(5, mask, want_energy=True)
         runs.append((s.get_positions(), s.get_velocities()))
     # (a re-sort after the restore changes partial-sum rounding only)

@@ -28,13 +28,15 @@ def _box():
     return systems.water_box(5000, 53.0, seed=21)   # 15,000 atoms, 8 x 8 columns
 
 
+@pytest.mark.parametrize("half", [0, 1])
 @pytest.mark.parametrize("rc", [10.0, 14.0, 20.0])
-def test_column_pair_set_equals_bruteforce(lib, orc, rc):
+def test_column_pair_set_equals_bruteforce(lib, orc, rc, half):
     w = _box()
     n = w.num_particles
     none = np.full((n, 1), -1)
     s = make_system(lib, n, w.box, lj=water_lj_rows(w), charges=np.zeros(n), bonded=none,
                     cutoff=rc, coulomb=lib.COUL_EWALD, beta=0.3, positions=w.positions)
+    s.set_launch_shape(half=half)
     gpu = pairs_to_set(s.pairset())
     bf = pairs_to_set(orc.pairs_bruteforce(w.positions, w.box, rc))
     _same_pairs(gpu, bf, w.positions, w.box, rc)
@@ -44,8 +46,9 @@ def test_column_pair_set_equals_bruteforce(lib, orc, rc):
     assert s.nonbonded_stats()["pairs_in_cutoff"] == len(gpu)
 
 
+@pytest.mark.parametrize("half", [0, 1])
 @pytest.mark.parametrize("n_waters,edge", [(5000, 53.0), (900, 30.0)])
-def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge):
+def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge, half):
     """400 Langevin steps at 900 K with no re-sort: unbonded H atoms fly
     tens of A, past the periodic box; the pair set still equals brute force
     (53 A: neighbour-column search; 30 A: full scan with 27 images)."""
@@ -59,6 +62,7 @@ def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge):
                     velocities=systems.maxwell_boltzmann(np.random.default_rng(3),
                                                          w.topology.masses, 900.0))
     s.set_reorder_interval(100000)
+    s.set_launch_shape(half=half)
     s.integrator_config(lib.INTEGRATOR_LANGEVIN, 1.0, 900.0, 0.001, 7)
     s.integrate(400, lib.mask(lib.TERM_LJ), want_energy=False)
     x = s.get_positions()
@@ -67,7 +71,8 @@ def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge):
     _same_pairs(gpu, bf, x, w.box, 12.0)
 
 
-def test_column_forces_vs_oracle(lib, orc):
+@pytest.mark.parametrize("half", [0, 1])
+def test_column_forces_vs_oracle(lib, orc, half):
     w = _box()
     t = w.topology
     n = w.num_particles
@@ -76,6 +81,7 @@ def test_column_forces_vs_oracle(lib, orc):
     s = make_system(lib, n, w.box, charges=t.charges.reshape(-1), lj=lj,
                     bonded=t.bonded_particles, scaling=t.scaling_particles, cutoff=12.0,
                     switch=10.0, coulomb=lib.COUL_EWALD, beta=beta, positions=w.positions)
+    s.set_launch_shape(half=half)
     s.compute_forces(lib.mask(lib.TERM_LJ, lib.TERM_COUL_REAL))
     f = s.get_forces()
     e, _ = s.get_energies()

@@ -222,3 +222,39 @@ def test_pdb_dumper_writes_fixed_column_frames(tmp_path):
     xyz = np.array([[float(ln[30:38]), float(ln[38:46]), float(ln[46:54])] for ln in atoms])
     assert np.allclose(xyz, np.concatenate(frames), atol=5e-4)
     assert atoms[1][12:16].strip() == "HT" and int(atoms[59][6:11]) == 60
+
+
+def test_charmm_forcefield_emits_device_constraints(monkeypatch):
+    """CharmmForcefield.create_ensemble (mdpy/forcefield/charmm_forcefield.py:96-112):
+    parameter check, and the constraint set for each long-range solver."""
+    from mdpy_gb300 import constraint as C, forcefield, systems
+    from mdpy_gb300.error import ParameterPoorDefinedError
+
+    class FakeEnsemble:
+        def __init__(self, topology, pbc, device=None):
+            self.cons = []
+
+        def add_constraints(self, *cons):
+            self.cons.extend(cons)
+
+    monkeypatch.setattr(forcefield, "Ensemble", FakeEnsemble)
+    w = systems.water_box(30, 14.0, seed=0)
+    ff = forcefield.CharmmForcefield(w.topology, w.pbc_matrix, cutoff_radius=6.0)
+    with pytest.raises(ParameterPoorDefinedError):
+        ff.check_parameters()
+    bad = {k: dict(v) for k, v in w.parameters.items()}
+    bad["nonbonded"].pop("HT")
+    ff.set_parameters(bad)
+    with pytest.raises(ParameterPoorDefinedError, match="HT"):
+        ff.check_parameters()
+    ff.set_parameters(w.parameters)
+    kinds = [type(c) for c in ff.create_ensemble().cons]
+    assert kinds == [C.NonbondedConstraint, C.PMEConstraint, C.CharmmBondConstraint,
+                     C.CharmmAngleConstraint]
+    ff2 = forcefield.CharmmForcefield(w.topology, w.pbc_matrix, cutoff_radius=6.0,
+                                      long_range_solver=None)
+    ff2.set_parameters(w.parameters)
+    kinds = [type(c) for c in ff2.create_ensemble().cons]
+    assert kinds[:2] == [C.ElectrostaticConstraint, C.CharmmNonbondedConstraint]
+    with pytest.raises(ValueError):
+        forcefield.CharmmForcefield(w.topology, w.pbc_matrix, long_range_solver="EWALD")
