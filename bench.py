@@ -55,6 +55,9 @@ def parse():
                         "waters (1M atoms) in a 215 A box; batch256: 256 independent water "
                         "boxes of 1.5k-12k atoms in one batch")
     p.add_argument("--boxes", type=int, default=256)
+    p.add_argument("--mts", default="2,4",
+                   help="outer steps (in steps) of the multiple-time-step forms timed beside the "
+                        "plain one, comma separated (empty: none)")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch shape instead of timing the alternatives")
     p.add_argument("--waters", type=int, default=None)
@@ -347,16 +350,18 @@ def barrier(world):
         dist.barrier()
 
 
-def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0):
+def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0, mts=1):
     """Total-energy drift of a velocity-Verlet run of ``ps`` picoseconds:
     ``equilibrate_ps`` of Langevin at 300 K first (the lattice start relaxes
     for several ps, which shows as a spurious trend), then the least-squares
     slope of E(t), sampled every ``chunk`` steps, in kT per ns per atom."""
     from mdpy_gb300 import _lib, unit
 
+    sysm.set_mts(1)
     sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 77 + seed)
     sysm.integrate(int(equilibrate_ps * 1000.0 / DT_FS), mask, want_energy=False)
     sysm.integrator_config(_lib.INTEGRATOR_VERLET, DT_FS)
+    sysm.set_mts(mts)
     n_chunks = max(2, int(round(ps * 1000.0 / DT_FS / chunk)))
     terms = [t for t in range(_lib.NUM_TERMS) if mask >> t & 1]
     t_fs, e_tot = [], []
@@ -375,11 +380,13 @@ def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0):
     halves = [float(np.polyfit(np.array(t_fs[i:j]), np.array(e_tot[i:j]), 1)[0]) * 1e6
               / (n_atoms * kT) for i, j in ((0, half), (half, n_chunks))]
     return {"kT_per_ns_per_atom": drift, "halves_kT_per_ns_per_atom": halves,
+            "noise_kT_per_ns_per_atom": abs(halves[0] - halves[1]) / 2.0,
             "ps": n_chunks * chunk * DT_FS / 1000.0,
             "samples": n_chunks, "sample_every_steps": chunk,
             "max_abs_dev_kT_per_atom": float(np.max(np.abs(np.array(e_tot) - e0)) / (n_atoms * kT)),
-            "integrator": "velocity Verlet, dt 1 fs, after %g ps of Langevin at 300 K"
-                          % equilibrate_ps,
+            "integrator": "velocity Verlet, dt 1 fs%s, after %g ps of Langevin at 300 K"
+                          % ((", reciprocal force every %d steps (impulse)" % mts) if mts > 1
+                             else "", equilibrate_ps),
             "wall_s": wall}
 
 
@@ -666,7 +673,26 @@ def main():
                  "pme_share_of_step": 1.0 - ms_no_pme / ms_step,
                  "max_saving_pme_every_4_steps": 0.75 * (1.0 - ms_no_pme / ms_step)}
 
+    # the multiple-time-step forms: same shape and protocol, PME every k steps
+    forms = []
+    for k in [int(t) for t in str(a.mts).split(",") if t.strip() and int(t) > 1]:
+        sysm.set_mts(k)
+        sysm.integrate(2 * k + 3, mask, want_energy=False)
+        reps = max(8 * k, (a.steps // (2 * k)) * k)
+        ms_k = time_steps(sysm, mask, reps, stream, flush) / reps
+        sysm.set_mts(1)
+        sysm.integrate(5, mask, want_energy=False)
+        forms.append({"form": "impulse multiple time steps: PME force every %d steps, weight %d "
+                              "(learned correction not built)" % (k, k), "mts": k,
+                      "ms_per_step": ms_k,
+                      "ns_per_day": unit.ns_per_day(world * 1000.0 / ms_k, DT_FS),
+                      "atom_steps_per_s": n * world * 1000.0 / ms_k, "timed_steps": reps})
+
     nve = nve_drift(sysm, mask, n, a.nve_ps) if a.nve_ps > 0 else None
+    if a.nve_ps > 0:
+        for f in forms:
+            f["nve_drift"] = nve_drift(sysm, mask, n, a.nve_ps / 2, mts=f["mts"], seed=1)
+        sysm.set_mts(1)
 
     err = None
     cpu = None
@@ -680,7 +706,14 @@ def main():
                    "atom_steps_per_s": r["atom_steps_per_s"]}
 
     if rank == 0:
-        plain = {"ns_per_day": value, "atom_steps_per_s": n * sps_job, "ms_per_step": ms_step}
+        plain = {"form": "plain", "ns_per_day": value, "atom_steps_per_s": n * sps_job,
+                 "ms_per_step": ms_step, "nve_drift": nve}
+        # the chosen form: the fastest whose NVE drift (when measured) is
+        # within 1e-3 kT/ns/atom
+        def within(f):
+            d = f.get("nve_drift")
+            return d is None or abs(d["kT_per_ns_per_atom"]) <= 1e-3
+        chosen = max([plain] + [f for f in forms if within(f)], key=lambda f: f["ns_per_day"])
         line = {
             "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_step,
@@ -695,7 +728,7 @@ def main():
             "force_rel_rms_err_vs_fp64": err,
             "nve_drift": nve,
             "mts_bound": mts_bound,
-            "plain": plain, "chosen": dict(plain, form="plain"),
+            "plain": plain, "chosen": chosen, "forms": forms,
             "roofline": roofline, "stages_ms": stage_ms, "nonbonded_stats": stats,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clk,

@@ -246,6 +246,15 @@ MDG_API int mdg_minimize_step(mdg_system *sys, double alpha);
 MDG_API int mdg_kinetic_energies_noalloc(mdg_system *sys, double *kinetic);
 
 /* ---- integration ------------------------------------------------------- */
+/* Multiple time steps (no reference counterpart): with k > 1 the
+ * reciprocal-space force (PME and the excluded-pair correction) enters only
+ * the evaluation that ends every k-th step, weighted by k, and is left out of
+ * the others -- the impulse (Verlet-I / r-RESPA) scheme with an outer step of
+ * k dt; the other terms are evaluated every step.  Energies stay complete
+ * (the reciprocal energy is computed on energy steps whatever the phase);
+ * mdg_get_forces after mdg_integrate returns the weighted buffer.  k = 1
+ * (default) is the ordinary integrator. */
+MDG_API int mdg_set_mts(mdg_system *sys, int k);
 /* VerletIntegrator / LangevinIntegrator (mdpy/integrator/*.py) re-designed:
  * velocity Verlet or Groenbech-Jensen--Farago Langevin, FP64 x/v, one force
  * evaluation per step, Philox4x32-10 noise keyed by (seed, atom, step). */

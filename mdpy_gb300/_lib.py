@@ -76,6 +76,7 @@ SIGNATURES = {
     "mdg_kinetic_energy": [_sys_p, _c_dbl_p],
     "mdg_kinetic_energies_noalloc": [_sys_p, _c_dbl_p],
     "mdg_minimize_step": [_sys_p, ctypes.c_double],
+    "mdg_set_mts": [_sys_p, ctypes.c_int],
     "mdg_step_host": [_sys_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint,
                       ctypes.c_void_p, ctypes.c_void_p, _c_dbl_p, _c_dbl_p],
     "mdg_set_launch_shape": [_sys_p, _c_int_p],
@@ -351,6 +352,10 @@ class System:
             None if energies is None else _dp(energies),
             ctypes.byref(ke) if want_kinetic else None))
         return ke.value
+
+    def set_mts(self, k):
+        """Reciprocal-space force every k-th step, weighted k (impulse MTS)."""
+        check(self._lib.mdg_set_mts(self._h, int(k)))
 
     def minimize_step(self, alpha):
         check(self._lib.mdg_minimize_step(self._h, float(alpha)))

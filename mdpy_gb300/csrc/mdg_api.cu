@@ -78,8 +78,9 @@ void drop_one(Graph &g) {
 
 void drop_graph(mdg_system *s) {
     drop_one(s->graph);
-    for (auto &row : s->graph_step)
-        for (Graph &g : row) drop_one(g);
+    for (auto &plane : s->graph_step)
+        for (auto &row : plane)
+            for (Graph &g : row) drop_one(g);
     for (Graph &g : s->graph_eval) drop_one(g);
 }
 
@@ -182,6 +183,9 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
     int rc = MDG_OK;
     cudaError_t e = cudaSuccess;
     s->stream = s->side_stream;
+    // (multiple time steps: weight 0 leaves the reciprocal force out, and the
+    // term runs at all only when its energy is wanted)
+    if (s->recip_weight == 0.f && !energy) mask &= ~MDG_MASK(MDG_TERM_COUL_RECIP);
     if ((mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on) {
         int cr = 0;
         e = launch_pme(s, energy, &cr);
@@ -204,12 +208,22 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
     return MDG_OK;
 }
 
+// weight of the reciprocal force in the evaluation that ends step `step`:
+// mts_k at the end of an outer step of the multiple-time-step scheme, else 0
+float mts_weight(const mdg_system *s, uint64_t step) {
+    if (s->mts_k <= 1) return 1.0f;
+    return ((step + 1) % (uint64_t)s->mts_k == 0) ? (float)s->mts_k : 0.0f;
+}
+
 int md_step(mdg_system *s, unsigned mask, int energy) {
     // (the pre-force update stays its own coalesced pass over atom order: a
     // version fused into the cluster-order packing measured 1 % slower)
     CK(launch_integrate_pre(s), "integrate pre");
     if (s->steps_since_reorder >= s->reorder_interval) s->need_reorder = 1;
+    s->recip_weight = mts_weight(s, s->step);
     int rc = evaluate(s, mask, energy);
+    s->forces_weight = s->recip_weight;
+    s->recip_weight = 1.0f;
     if (rc) return rc;
     CK(launch_integrate_post(s, energy), "integrate post");
     s->steps_since_reorder += 1;
@@ -914,6 +928,7 @@ MDG_API int mdg_compute_forces(mdg_system *s, unsigned mask) {
     if (rc) return rc;
     s->forces_valid = 1;
     s->forces_mask = mask;
+    s->forces_weight = 1.0f;
     CK(cudaGetLastError(), "compute forces");
     return MDG_OK;
 }
@@ -1314,6 +1329,16 @@ MDG_API int mdg_step_host(mdg_system *s, const double *x_in, const double *v_in,
     return MDG_OK;
 }
 
+MDG_API int mdg_set_mts(mdg_system *s, int k) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (k < 1 || k > 16) return fail(MDG_ERR_INVALID, "outer step %d not in 1..16", k);
+    s->mts_k = k;
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
 MDG_API int mdg_integrator_config(mdg_system *s, int kind, double dt, double temperature,
                                   double friction, uint64_t seed) {
     int rc = check_sys(s);
@@ -1359,13 +1384,24 @@ MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_en
     if (rc) return rc;
     if (!s->have_masses) return fail(MDG_ERR_STATE, "masses have not been set");
     if (s->graph.exec && s->graph.mask != mask) drop_graph(s);
-    for (auto &row : s->graph_step)
-        for (Graph &g : row)
-            if (g.exec && g.mask != mask) drop_graph(s);
+    for (auto &plane : s->graph_step)
+        for (auto &row : plane)
+            for (Graph &g : row)
+                if (g.exec && g.mask != mask) drop_graph(s);
     for (Graph &g : s->graph_eval)
         if (g.exec && g.mask != mask) drop_graph(s);
-    if (!s->forces_valid || s->forces_mask != mask) {
-        if (s->graph_mode == MDG_GRAPH_STEP && n_steps > 0) {
+    // the force buffer the first pre-force update uses: multiple time steps
+    // want the weight of the evaluation that ended the previous step
+    const float want_w = s->step == 0 ? mts_weight(s, (uint64_t)s->mts_k - 1)
+                                      : mts_weight(s, s->step - 1);
+    if (!s->forces_valid || s->forces_mask != mask || s->forces_weight != want_w) {
+        if (s->mts_k > 1) {
+            s->recip_weight = want_w;
+            rc = evaluate(s, mask, 0);
+            s->recip_weight = 1.0f;
+            if (rc) return rc;
+            s->forces_weight = want_w;
+        } else if (s->graph_mode == MDG_GRAPH_STEP && n_steps > 0) {
             const int resort = s->need_reorder ? 1 : 0;
             Graph &g = s->graph_eval[resort];
             if (!g.exec) {
@@ -1390,9 +1426,10 @@ MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_en
     while (remaining > 0) {
         const bool chunk_start = s->need_reorder || s->steps_since_reorder >= R;
         const int usable = remaining - (want_energy ? 1 : 0);
-        if (s->graph_mode == MDG_GRAPH_STEP) {
+        if (s->graph_mode == MDG_GRAPH_STEP || s->mts_k > 1) {
             const int e = (want_energy && remaining == 1) ? 1 : 0;
-            Graph &g = s->graph_step[chunk_start ? 1 : 0][e];
+            const int outer = mts_weight(s, s->step) != 0.f ? 1 : 0;
+            Graph &g = s->graph_step[chunk_start ? 1 : 0][e][outer];
             if (!g.exec) {
                 rc = capture_steps(s, g, 1, chunk_start, mask, e);
                 if (rc) return rc;
@@ -1401,6 +1438,7 @@ MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_en
             s->launches += g.steps;
             s->need_reorder = 0;
             s->steps_since_reorder = chunk_start ? 1 : s->steps_since_reorder + 1;
+            s->forces_weight = mts_weight(s, s->step);
             s->step += 1;
             remaining -= 1;
         } else if (chunk_start && usable >= R && R >= 2) {
@@ -1424,6 +1462,7 @@ MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_en
     if (want_energy && n_steps == 0) {
         rc = evaluate(s, mask, 1);
         if (rc) return rc;
+        s->forces_weight = 1.0f;
     }
     s->forces_valid = 1;
     s->forces_mask = mask;

@@ -351,6 +351,12 @@ struct mdg_system {
     int pme_tiles = 0;                // bit 0: tiled spread, bit 1: tiled gather
     int nb_half = 0;                  // 1: 16-atom i groups per half warp
 
+    // multiple time steps (impulse): the reciprocal-space force enters every
+    // mts_k-th evaluation with weight mts_k and is skipped in between
+    int mts_k = 1;
+    float recip_weight = 1.0f;        // weight of the reciprocal force in the next evaluation
+    float forces_weight = 1.0f;       // weight in the force buffer's evaluation
+
     // nonbonded configuration
     float cutoff = 12.0f, rswitch = 0.0f;
     int lj_on = 1, coul_mode = MDG_COUL_NONE;
@@ -385,7 +391,7 @@ struct mdg_system {
     unsigned forces_mask = 0;
     long long launches = 0;
     mdg::Graph graph;                  // chunk of reorder_interval steps
-    mdg::Graph graph_step[2][2];       // one step: [re-sort first][with energies]
+    mdg::Graph graph_step[2][2][2];    // one step: [re-sort first][with energies][MTS outer boundary]
     mdg::Graph graph_eval[2];          // the evaluation before a first step: [re-sort first]
     int graph_mode = 0;
 

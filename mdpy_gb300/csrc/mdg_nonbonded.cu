@@ -122,6 +122,7 @@ struct SpArgs {
     int n_excl, n_14, n_pad;
     float rc2, rs2, sw_inv_den, beta, ewald_fc;
     int do_excl, do_lj14, do_coul14;
+    float excl_weight;  // weight of the excluded-pair reciprocal correction's force
     unsigned long long *f;
     long long *energy;
     int *dump;
@@ -159,7 +160,7 @@ __global__ void k_special(SpArgs a) {
                 const float br = a.beta * r;
                 const float ef = erff(br);
                 e_rec = -qq * ef / r;
-                fr = qq * (a.ewald_fc * expf(-br * br) * r - ef) / (r2 * r);
+                fr = a.excl_weight * qq * (a.ewald_fc * expf(-br * br) * r - ef) / (r2 * r);
             }
         } else if (r2 <= a.rc2) {
             if (DUMP) {
@@ -307,6 +308,7 @@ cudaError_t launch_special(mdg_system *s, unsigned mask, int energy, int dump) {
     a.beta = (float)s->beta;
     a.ewald_fc = (float)(2.0 * s->beta / 1.7724538509055159);
     a.do_excl = (mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on && !dump;
+    a.excl_weight = s->recip_weight;
     a.do_lj14 = (mask & MDG_MASK(MDG_TERM_LJ)) && s->lj_on;
     a.do_coul14 = (mask & MDG_MASK(MDG_TERM_COUL_REAL)) && s->coul_mode == MDG_COUL_EWALD;
     a.f = s->f;

@@ -71,6 +71,7 @@ struct PmeArgs {
     const float *__restrict__ phi;
     unsigned long long *f;
     int tile_spread, tile_gather;  // stage the block's grid patch in shared memory
+    float weight;                  // force weight (multiple time steps)
 };
 
 // grid coordinate u = x K / L wrapped into [0, K) with fmodf (exact), so the
@@ -359,9 +360,9 @@ __global__ void __launch_bounds__(256) k_gather(PmeArgs a) {
             fz = fmaf(th[0][i] * th[1][j], sdz, fz);
         }
     }
-    fx *= -p.w * kl[0];
-    fy *= -p.w * kl[1];
-    fz *= -p.w * kl[2];
+    fx *= -p.w * kl[0] * a.weight;
+    fy *= -p.w * kl[1] * a.weight;
+    fz *= -p.w * kl[2] * a.weight;
     fix_red(&a.f[k], to_fix(fx));
     fix_red(&a.f[a.n_pad + k], to_fix(fy));
     fix_red(&a.f[2 * a.n_pad + k], to_fix(fz));
@@ -552,6 +553,7 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
     a.f = s->f;
     a.tile_spread = s->pme_tiles & 1;
     a.tile_gather = (s->pme_tiles >> 1) & 1;
+    a.weight = s->recip_weight;
     const int tb = 256;
     const int ab = s->pme_block, nb = (s->n_pad + ab - 1) / ab;  // per-atom kernels
     // dynamic shared memory only for the kernels that stage a tile (it limits
@@ -601,13 +603,15 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
             return cudaGetLastError();
         }
     }
-    switch (p.order) {
-        case 4: k_gather<4><<<nb, ab, gather_smem, st>>>(a); break;
-        case 5: k_gather<5><<<nb, ab, gather_smem, st>>>(a); break;
-        case 6: k_gather<6><<<nb, ab, gather_smem, st>>>(a); break;
-        default: break;
+    if (a.weight != 0.f) {  // weight 0: the energy alone
+        switch (p.order) {
+            case 4: k_gather<4><<<nb, ab, gather_smem, st>>>(a); break;
+            case 5: k_gather<5><<<nb, ab, gather_smem, st>>>(a); break;
+            case 6: k_gather<6><<<nb, ab, gather_smem, st>>>(a); break;
+            default: break;
+        }
+        s->launches += 1;
     }
-    s->launches += 1;
     return cudaGetLastError();
 }
 

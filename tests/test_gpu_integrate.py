@@ -197,3 +197,76 @@ def test_step_host_equals_separate_calls(lib):
     keb2 = b.step_host_ptr(0, 0, 3, mask, xb.ctypes.data, 0, eb)
     a.integrate(3, mask, want_energy=True)
     assert np.array_equal(a.get_positions(), xb) and a.get_energies()[1] == keb2
+
+
+def test_mts_impulse_equations(lib):
+    """Multiple time steps, k = 2: the steps follow the impulse (Verlet-I)
+    equations restated in numpy from the library's own term forces -- the
+    reciprocal force enters with weight 2 at the end of every second step and
+    is absent in between."""
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(900, 30.0, seed=0)
+    ens = _ensemble(w)
+    probe = _ensemble(w)   # term forces at given positions
+    s, mask = ens.system, ens.term_mask
+    recip = lib.mask(lib.TERM_COUL_RECIP)
+    fast = mask & ~recip
+    m = w.topology.masses.reshape(-1, 1)
+
+    def forces(x, terms):
+        probe.system.set_positions(x)
+        probe.system.compute_forces(terms)
+        return probe.system.get_forces()
+
+    x, v = w.positions.copy(), w.velocities.copy()
+    s.set_positions(x)
+    s.set_velocities(v)
+    s.integrator_config(lib.INTEGRATOR_VERLET, 1.0)
+    s.set_mts(2)
+    f = forces(x, fast) + 2.0 * forces(x, recip)      # the outer step starts with the impulse
+    for step in range(4):
+        s.integrate(1, mask, want_energy=False)
+        x = x + v + 0.5 * f / m
+        vh = v + 0.5 * f / m
+        f = forces(x, fast) + (2.0 * forces(x, recip) if step % 2 == 1 else 0.0)
+        v = vh + 0.5 * f / m
+        d = s.get_positions() - x
+        d -= w.box * np.round(d / w.box)
+        # (a wrong weight would be off by ~1e-3 A; float rounding of the
+        # probe's forces leaves ~1e-8)
+        assert np.abs(d).max() < 1e-7, step
+        # (the probe's forces round differently from the running system's:
+        # other cluster layouts, FP32 partial sums)
+        assert np.abs(s.get_velocities() - v).max() < 2e-6 * np.abs(v).max(), step
+    # k = 1 is the ordinary integrator, bit for bit
+    a, b = _ensemble(w), _ensemble(w)
+    for e in (a, b):
+        e.system.integrator_config(lib.INTEGRATOR_VERLET, 1.0)
+    a.system.set_mts(1)
+    a.system.integrate(10, mask, want_energy=True)
+    b.system.integrate(10, mask, want_energy=True)
+    assert np.array_equal(a.system.get_positions(), b.system.get_positions())
+    assert np.array_equal(a.system.get_energies()[0], b.system.get_energies()[0])
+
+
+def test_mts_energy_reported_at_inner_steps(lib):
+    """Energies of a multiple-time-step run include the reciprocal term on
+    every energy step, outer or inner."""
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(900, 30.0, seed=1)
+    ens = _ensemble(w)
+    s, mask = ens.system, ens.term_mask
+    s.integrator_config(lib.INTEGRATOR_VERLET, 1.0)
+    s.set_mts(4)
+    for n in (1, 2, 3, 4):
+        s.integrate(1, mask, want_energy=True)
+        e, _ = s.get_energies()
+        x = s.get_positions()
+        probe = _ensemble(w)
+        probe.system.set_positions(x)
+        probe.system.compute_forces(mask)
+        ep, _ = probe.system.get_energies()
+        assert abs(e[lib.TERM_COUL_RECIP] - ep[lib.TERM_COUL_RECIP]) < 1e-6 * abs(ep[lib.TERM_COUL_RECIP]) + 1e-6
+        probe.system.close()
