@@ -58,6 +58,14 @@ def parse():
     p.add_argument("--mts", default="2,4",
                    help="outer steps (in steps) of the multiple-time-step forms timed beside the "
                         "plain one, comma separated (empty: none)")
+    p.add_argument("--learned", default="4",
+                   help="outer steps of the learned slow-force forms (trained at the start, "
+                        "comma separated; empty: none)")
+    p.add_argument("--learned-iters", type=int, default=400,
+                   help="training iterations (frame pairs) of each learned form")
+    p.add_argument("--learned-threshold", type=float, default=5e-3,
+                   help="judge threshold of the learned forms (RMS slow-force error over RMS "
+                        "total force) above which an interval falls back to the impulse scheme")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch shape instead of timing the alternatives")
     p.add_argument("--waters", type=int, default=None)
@@ -350,7 +358,8 @@ def barrier(world):
         dist.barrier()
 
 
-def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0, mts=1):
+def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0, mts=1,
+              learned=None):
     """Total-energy drift of a velocity-Verlet run of ``ps`` picoseconds:
     ``equilibrate_ps`` of Langevin at 300 K first (the lattice start relaxes
     for several ps, which shows as a spurious trend), then the least-squares
@@ -361,7 +370,11 @@ def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0, m
     sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 77 + seed)
     sysm.integrate(int(equilibrate_ps * 1000.0 / DT_FS), mask, want_energy=False)
     sysm.integrator_config(_lib.INTEGRATOR_VERLET, DT_FS)
-    sysm.set_mts(mts)
+    if learned is not None:
+        learned.enable(sysm)
+        sysm.learned_reset_stats()
+    else:
+        sysm.set_mts(mts)
     n_chunks = max(2, int(round(ps * 1000.0 / DT_FS / chunk)))
     terms = [t for t in range(_lib.NUM_TERMS) if mask >> t & 1]
     t_fs, e_tot = [], []
@@ -372,6 +385,8 @@ def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0, m
         t_fs.append((k + 1) * chunk * DT_FS)
         e_tot.append(float(sum(e[t] for t in terms) + ke))
     wall = time.perf_counter() - t0
+    judge = sysm.learned_stats() if learned is not None else None
+    sysm.set_mts(1)
     slope = float(np.polyfit(np.array(t_fs), np.array(e_tot), 1)[0])   # energy unit / fs
     kT = unit.KB * TEMPERATURE
     drift = slope * 1e6 / (n_atoms * kT)
@@ -393,9 +408,11 @@ def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0, m
             "samples": n_chunks, "sample_every_steps": chunk,
             "max_abs_dev_kT_per_atom": float(np.max(np.abs(np.array(e_tot) - e0)) / (n_atoms * kT)),
             "integrator": "velocity Verlet, dt 1 fs%s, after %g ps of Langevin at 300 K"
-                          % ((", reciprocal force every %d steps (impulse)" % mts) if mts > 1
+                          % ((", learned slow force, PME every %d steps" % learned.outer_step)
+                             if learned is not None else
+                             (", reciprocal force every %d steps (impulse)" % mts) if mts > 1
                              else "", equilibrate_ps),
-            "wall_s": wall}
+            "judge": judge, "wall_s": wall}
 
 
 # --------------------------------------------------------------------------
@@ -690,16 +707,51 @@ def main():
         ms_k = time_steps(sysm, mask, reps, stream, flush) / reps
         sysm.set_mts(1)
         sysm.integrate(5, mask, want_energy=False)
-        forms.append({"form": "impulse multiple time steps: PME force every %d steps, weight %d "
-                              "(learned correction not built)" % (k, k), "mts": k,
+        forms.append({"form": "impulse multiple time steps: PME force every %d steps, weight %d"
+                              % (k, k), "mts": k,
                       "ms_per_step": ms_k,
                       "ns_per_day": unit.ns_per_day(world * 1000.0 / ms_k, DT_FS),
                       "atom_steps_per_s": n * world * 1000.0 / ms_k, "timed_steps": reps})
 
+    # the learned slow-force forms: trained here on frames of the plain
+    # method (Langevin, 280-320 K), then timed with the same protocol; the
+    # judge's statistics over the timed steps give the prediction's error
+    learned_forms = {}
+    for k in [int(t) for t in str(a.learned).split(",") if t.strip() and int(t) > 1]:
+        from mdpy_gb300.learned import LearnedSlowForce
+
+        lrn = LearnedSlowForce(outer_step=k, threshold=a.learned_threshold)
+        t_tr = time.perf_counter()
+        losses = lrn.train(sysm, iterations=a.learned_iters, lr=2e-3, seed=k, mask=mask)
+        t_tr = time.perf_counter() - t_tr
+        held = float(np.mean(losses[:5])) if losses else None
+        sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 4242 + k)
+        lrn.enable(sysm)
+        sysm.integrate(4 * k + 3, mask, want_energy=False)
+        sysm.learned_reset_stats()
+        reps = max(8 * k, (a.steps // (2 * k)) * k)
+        ms_k = time_steps(sysm, mask, reps, stream, flush) / reps
+        judge = sysm.learned_stats()
+        sysm.set_mts(1)
+        sysm.integrate(5, mask, want_energy=False)
+        f = {"form": "learned slow force: PME every %d steps, network prediction between, "
+                     "impulse fallback above a judged error of %g" % (k, a.learned_threshold),
+             "learned": k, "ms_per_step": ms_k,
+             "ns_per_day": unit.ns_per_day(world * 1000.0 / ms_k, DT_FS),
+             "atom_steps_per_s": n * world * 1000.0 / ms_k, "timed_steps": reps,
+             "judge_over_timed_steps": judge,
+             "training": {"iterations": a.learned_iters, "seconds": t_tr,
+                          "loss_first5": held, "loss_last20": float(np.mean(losses[-20:])),
+                          "loss": "sum |G(x1)-G(x0) - dF_slow|^2 / sum |dF_slow|^2 over frame "
+                                  "pairs 1..k steps apart (1 = holding the slow force)"}}
+        forms.append(f)
+        learned_forms[id(f)] = lrn
+
     nve = nve_drift(sysm, mask, n, a.nve_ps) if a.nve_ps > 0 else None
     if a.nve_ps > 0:
         for f in forms:
-            f["nve_drift"] = nve_drift(sysm, mask, n, a.nve_ps, mts=f["mts"], seed=1)
+            f["nve_drift"] = nve_drift(sysm, mask, n, a.nve_ps, mts=f.get("mts", 1), seed=1,
+                                       learned=learned_forms.get(id(f)))
         sysm.set_mts(1)
 
     err = None

@@ -255,6 +255,56 @@ MDG_API int mdg_kinetic_energies_noalloc(mdg_system *sys, double *kinetic);
  * mdg_get_forces after mdg_integrate returns the weighted buffer.  k = 1
  * (default) is the ordinary integrator. */
 MDG_API int mdg_set_mts(mdg_system *sys, int k);
+
+/* ---- learned slow force (no reference counterpart) ----------------------
+ * The multiple-time-step form with a learned prediction between full PME
+ * evaluations.  The slow force (PME plus the excluded-pair correction) is
+ * computed in full at every k-th step; in between it is predicted as
+ * F_slow(t0) + G(x(t)) - G(x(t0)), t0 the last full evaluation, where G is a
+ * rotation-equivariant network: per atom 64 invariant radial features of the
+ * neighbours within rf (sum_j q_j phi_b(r_ij) and sum_j phi_b(r_ij) over 32
+ * cubic B-spline bins), a BF16 MLP 64-128-128-16 (SiLU, FP32 accumulation)
+ * and G_i = sum_b C_ib q_i sum_j q_j psi_b(r_ij) (x_i - x_j) / rf^2 over 16
+ * radial functions psi_b.  Each full evaluation judges the prediction made
+ * for it (RMS error over RMS total force); above the threshold the next
+ * interval uses the impulse scheme of mdg_set_mts instead.  One system only.
+ *
+ * mdg_learned_config allocates the network's buffers: feature radius rf (A),
+ * neighbour-list skin (A), list entries per atom.  Parameters are one FP32
+ * vector of mdg_learned_num_params entries: feature shift [64], feature
+ * inverse scale [64], W1 [64][128], b1 [128], W2 [128][128], b2 [128],
+ * W3 [128][16], b3 [16], output scale [1] (weights [in][out]). */
+MDG_API int mdg_learned_config(mdg_system *sys, double rf, double skin, int list_capacity);
+MDG_API int mdg_learned_num_params(int32_t *n);
+MDG_API int mdg_learned_set_params(mdg_system *sys, const float *params, int32_t n);
+MDG_API int mdg_learned_get_params(mdg_system *sys, float *params, int32_t n);
+/* Training.  mdg_learned_frame(slot) evaluates the slow force at the current
+ * positions and runs the network forward, keeping what the backward pass
+ * needs (slots 0 and 1: two frames a few steps apart of a plain run);
+ * mdg_learned_frame_data copies a frame's raw features (n x 64), vector
+ * basis (n x 48, index 3 b + axis), slow force (n x 3) and prediction G
+ * (n x 3) to the host (any pointer may be null).  mdg_learned_train_step
+ * fits G(x1) - G(x0) to F_slow(x1) - F_slow(x0) over the two frames: loss =
+ * sum |residual|^2 / sum |F_slow(x1) - F_slow(x0)|^2 of the frames before
+ * the update (1 = no better than holding the slow force), one Adam step
+ * (beta 0.9 / 0.999, step number t >= 1, rate lr). */
+MDG_API int mdg_learned_frame(mdg_system *sys, int32_t slot);
+MDG_API int mdg_learned_frame_data(mdg_system *sys, int32_t slot, float *features, float *vectors,
+                                   float *slow_force, float *predicted);
+MDG_API int mdg_learned_train_step(mdg_system *sys, float lr, int32_t t, double *loss);
+/* the inference kernel (mdg_learned_set_kernel) on the features of a frame;
+ * G (n x 3) to the host when `predicted` is not null */
+MDG_API int mdg_learned_predict(mdg_system *sys, int32_t slot, float *predicted);
+/* k >= 2: use the learned form with outer step k and judge threshold;
+ * k = 0 or 1: off (and the impulse scheme off).  mdg_set_mts turns it off. */
+MDG_API int mdg_set_mts_learned(mdg_system *sys, int32_t k, double threshold);
+/* 1: the tcgen05 tensor-core MLP kernel for inference; 0: the SIMT kernel */
+MDG_API int mdg_learned_set_kernel(mdg_system *sys, int32_t tensor_cores);
+/* out[8]: last judged error, largest, sum of errors, judgements, fallbacks,
+ * last training loss, last training target norm, mode of the current
+ * interval (0 learned, 1 impulse fallback) */
+MDG_API int mdg_learned_stats(mdg_system *sys, double *out8);
+MDG_API int mdg_learned_reset_stats(mdg_system *sys);
 /* VerletIntegrator / LangevinIntegrator (mdpy/integrator/*.py) re-designed:
  * velocity Verlet or Groenbech-Jensen--Farago Langevin, FP64 x/v, one force
  * evaluation per step, Philox4x32-10 noise keyed by (seed, atom, step). */

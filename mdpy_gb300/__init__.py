@@ -27,8 +27,11 @@ def __getattr__(name):
     if name == "EnsembleBatch":
         from .batch import EnsembleBatch
         return EnsembleBatch
+    if name == "LearnedSlowForce":
+        from .learned import LearnedSlowForce
+        return LearnedSlowForce
     if name in ("constraint", "integrator", "simulation", "ensemble", "systems", "_lib",
-                "minimizer", "batch", "forcefield"):
+                "minimizer", "batch", "forcefield", "learned"):
         import importlib
         return importlib.import_module("." + name, __name__)
     raise AttributeError(name)
@@ -36,5 +39,5 @@ def __getattr__(name):
 
 __all__ = ["unit", "error", "Particle", "Topology", "Ensemble", "State", "Simulation",
            "SteepestDescentMinimizer", "ConjugateGradientMinimizer", "EnsembleBatch",
-           "constraint", "integrator", "simulation", "systems", "minimizer", "batch",
-           "forcefield"]
+           "LearnedSlowForce", "constraint", "integrator", "simulation", "systems", "minimizer",
+           "batch", "forcefield", "learned"]

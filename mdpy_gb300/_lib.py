@@ -77,6 +77,18 @@ SIGNATURES = {
     "mdg_kinetic_energies_noalloc": [_sys_p, _c_dbl_p],
     "mdg_minimize_step": [_sys_p, ctypes.c_double],
     "mdg_set_mts": [_sys_p, ctypes.c_int],
+    "mdg_learned_config": [_sys_p, ctypes.c_double, ctypes.c_double, ctypes.c_int],
+    "mdg_learned_num_params": [_c_i32_p],
+    "mdg_learned_set_params": [_sys_p, _c_f32_p, ctypes.c_int32],
+    "mdg_learned_get_params": [_sys_p, _c_f32_p, ctypes.c_int32],
+    "mdg_learned_frame": [_sys_p, ctypes.c_int32],
+    "mdg_learned_frame_data": [_sys_p, ctypes.c_int32, _c_f32_p, _c_f32_p, _c_f32_p, _c_f32_p],
+    "mdg_learned_train_step": [_sys_p, ctypes.c_float, ctypes.c_int32, _c_dbl_p],
+    "mdg_learned_predict": [_sys_p, ctypes.c_int32, _c_f32_p],
+    "mdg_set_mts_learned": [_sys_p, ctypes.c_int32, ctypes.c_double],
+    "mdg_learned_set_kernel": [_sys_p, ctypes.c_int32],
+    "mdg_learned_stats": [_sys_p, _c_dbl_p],
+    "mdg_learned_reset_stats": [_sys_p],
     "mdg_step_host": [_sys_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint,
                       ctypes.c_void_p, ctypes.c_void_p, _c_dbl_p, _c_dbl_p],
     "mdg_set_launch_shape": [_sys_p, _c_int_p],
@@ -356,6 +368,68 @@ class System:
     def set_mts(self, k):
         """Reciprocal-space force every k-th step, weighted k (impulse MTS)."""
         check(self._lib.mdg_set_mts(self._h, int(k)))
+
+    # ---- learned slow force -------------------------------------------------
+    @staticmethod
+    def learned_num_params():
+        n = ctypes.c_int32(0)
+        check(load().mdg_learned_num_params(ctypes.byref(n)))
+        return n.value
+
+    def learned_config(self, rf=6.0, skin=1.0, list_capacity=256):
+        check(self._lib.mdg_learned_config(self._h, float(rf), float(skin), int(list_capacity)))
+
+    def learned_set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32).ravel()
+        check(self._lib.mdg_learned_set_params(self._h, p.ctypes.data_as(_c_f32_p), p.size))
+
+    def learned_params(self):
+        p = np.zeros(self.learned_num_params(), dtype=np.float32)
+        check(self._lib.mdg_learned_get_params(self._h, p.ctypes.data_as(_c_f32_p), p.size))
+        return p
+
+    def learned_frame(self, slot):
+        check(self._lib.mdg_learned_frame(self._h, int(slot)))
+
+    def learned_frame_data(self, slot):
+        """(features n x 64, vectors n x 16 x 3, slow force n x 3, prediction n x 3)"""
+        n = self.n
+        feat = np.zeros((n, 64), dtype=np.float32)
+        vec = np.zeros((n, 16, 3), dtype=np.float32)
+        slow = np.zeros((n, 3), dtype=np.float32)
+        pred = np.zeros((n, 3), dtype=np.float32)
+        check(self._lib.mdg_learned_frame_data(
+            self._h, int(slot), feat.ctypes.data_as(_c_f32_p), vec.ctypes.data_as(_c_f32_p),
+            slow.ctypes.data_as(_c_f32_p), pred.ctypes.data_as(_c_f32_p)))
+        return feat, vec, slow, pred
+
+    def learned_predict(self, slot=0):
+        """G (n x 3) of the inference kernel on the features of a frame"""
+        out = np.zeros((self.n, 3), dtype=np.float32)
+        check(self._lib.mdg_learned_predict(self._h, int(slot), out.ctypes.data_as(_c_f32_p)))
+        return out
+
+    def learned_train_step(self, lr, t):
+        loss = ctypes.c_double(0.0)
+        check(self._lib.mdg_learned_train_step(self._h, float(lr), int(t), ctypes.byref(loss)))
+        return loss.value
+
+    def set_mts_learned(self, k, threshold=1e-3):
+        check(self._lib.mdg_set_mts_learned(self._h, int(k), float(threshold)))
+
+    def learned_set_kernel(self, tensor_cores):
+        check(self._lib.mdg_learned_set_kernel(self._h, int(bool(tensor_cores))))
+
+    def learned_stats(self):
+        out = np.zeros(8)
+        check(self._lib.mdg_learned_stats(self._h, _dp(out)))
+        return {"last_err": out[0], "max_err": out[1],
+                "mean_err": out[2] / out[3] if out[3] else 0.0, "judged": int(out[3]),
+                "fallbacks": int(out[4]), "loss": out[5], "target_norm": out[6],
+                "mode": "impulse" if out[7] else "learned"}
+
+    def learned_reset_stats(self):
+        check(self._lib.mdg_learned_reset_stats(self._h))
 
     def minimize_step(self, alpha):
         check(self._lib.mdg_minimize_step(self._h, float(alpha)))

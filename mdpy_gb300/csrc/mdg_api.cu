@@ -172,6 +172,11 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
         CK(cudaMemsetAsync(s->stats, 0, sizeof(unsigned long long) * 4, s->stream), "memset");
     }
     CK(launch_pack(s), "pack");
+    const int lsp = s->ls ? s->ls_phase : kLsOff;
+    if (lsp >= kLsOuter)  // full evaluation of the learned form: slow force kept apart
+        CK(cudaMemsetAsync(s->ls->fs, 0, sizeof(unsigned long long) * 3 * (size_t)s->n_pad,
+                           s->stream),
+           "memset");
     // fork: PME on one side stream, special pairs and bonded terms on
     // another, while the pair kernel runs on the main stream (all accumulate
     // through order-independent fixed-point atomics); join both before
@@ -191,6 +196,8 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
         e = launch_pme(s, energy, &cr);
         if (cr != CUFFT_SUCCESS) rc = fail(MDG_ERR_CUFFT, "cuFFT execution failed (%d)", cr);
     }
+    // learned slow force: features and MLP after PME on the same stream
+    if (!rc && e == cudaSuccess && lsp != kLsOff) e = ls_side(s, lsp);
     cudaError_t ej = cudaEventRecord(s->ev_join, s->side_stream);
     s->stream = s->bond_stream;
     if (!rc && e == cudaSuccess) e = launch_special(s, mask, energy, 0);
@@ -204,8 +211,26 @@ int evaluate(mdg_system *s, unsigned mask, int energy) {
     CK(launch_nonbonded(s, mask, energy, 0), "nonbonded");
     CK(cudaStreamWaitEvent(s->stream, s->ev_join, 0), "join wait");
     CK(cudaStreamWaitEvent(s->stream, s->ev_join2, 0), "join wait");
+    if (lsp != kLsOff) CK(ls_after_join(s, lsp), "learned slow force");
     s->evaluated_once = 1;
     return MDG_OK;
+}
+
+bool ls_active(const mdg_system *s) { return s->ls && s->ls->enabled; }
+
+// One evaluation of the learned form (phase kLsInner / kLsOuter / kLsAnchor):
+// PME only at full evaluations, into the slow-force buffer.
+int ls_evaluate(mdg_system *s, unsigned mask, int energy, int phase) {
+    const bool full = phase != kLsInner;
+    s->ls_phase = phase;
+    s->recip_weight = full ? 1.0f : 0.0f;
+    s->slow_target = full ? s->ls->fs : nullptr;
+    const int rc = evaluate(s, mask, energy);
+    s->ls_phase = kLsOff;
+    s->slow_target = nullptr;
+    s->recip_weight = 1.0f;
+    s->forces_weight = -1.0f;
+    return rc;
 }
 
 // weight of the reciprocal force in the evaluation that ends step `step`:
@@ -220,10 +245,15 @@ int md_step(mdg_system *s, unsigned mask, int energy) {
     // version fused into the cluster-order packing measured 1 % slower)
     CK(launch_integrate_pre(s), "integrate pre");
     if (s->steps_since_reorder >= s->reorder_interval) s->need_reorder = 1;
-    s->recip_weight = mts_weight(s, s->step);
-    int rc = evaluate(s, mask, energy);
-    s->forces_weight = s->recip_weight;
-    s->recip_weight = 1.0f;
+    int rc;
+    if (ls_active(s)) {
+        rc = ls_evaluate(s, mask, energy, mts_weight(s, s->step) != 0.f ? kLsOuter : kLsInner);
+    } else {
+        s->recip_weight = mts_weight(s, s->step);
+        rc = evaluate(s, mask, energy);
+        s->forces_weight = s->recip_weight;
+        s->recip_weight = 1.0f;
+    }
     if (rc) return rc;
     CK(launch_integrate_post(s, energy), "integrate post");
     s->steps_since_reorder += 1;
@@ -511,6 +541,7 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->dih_prm);
     dfree(s->imp_idx);
     dfree(s->imp_prm);
+    ls_free(s);
     for (cudaStream_t *pair : {s->side_streams, s->bond_streams})
         for (int k = 0; k < 2; ++k)
             if (pair[k]) {
@@ -563,6 +594,17 @@ MDG_API int mdg_system_set_boxes(mdg_system *s, const double *boxes) {
         rc = pme_setup(s, grids.data());
         if (rc) return fail(rc, "PME set-up failed");
         ewald_constants(s);
+    }
+    if (s->ls) {  // the learned form's cell grid follows the box (parameters kept)
+        const Learned &L = *s->ls;
+        const int on = L.enabled, k = L.k, tc = L.use_tc, cap = L.cap;
+        const float thr = L.threshold, rf = L.rf, skin = L.skin;
+        rc = ls_configure(s, rf, skin, cap);
+        if (rc) return fail(rc, "learned slow force: box too small or allocation failed");
+        s->ls->enabled = on;
+        s->ls->k = k;
+        s->ls->threshold = thr;
+        s->ls->use_tc = tc;
     }
     s->need_reorder = 1;
     s->forces_valid = 0;
@@ -1334,8 +1376,201 @@ MDG_API int mdg_set_mts(mdg_system *s, int k) {
     if (rc) return rc;
     if (k < 1 || k > 16) return fail(MDG_ERR_INVALID, "outer step %d not in 1..16", k);
     s->mts_k = k;
+    if (s->ls) s->ls->enabled = 0;
     s->forces_valid = 0;
     drop_graph(s);
+    return MDG_OK;
+}
+
+// ---- learned slow force ------------------------------------------------------
+
+MDG_API int mdg_learned_config(mdg_system *s, double rf, double skin, int list_capacity) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (s->n_sys != 1) return fail(MDG_ERR_INVALID, "the learned slow force takes one system");
+    if (!(rf >= 2.0 && rf <= 12.0)) return fail(MDG_ERR_INVALID, "rf %g not in [2, 12] A", rf);
+    if (!(skin >= 0.0 && skin <= 4.0)) return fail(MDG_ERR_INVALID, "skin %g not in [0, 4] A", skin);
+    if (list_capacity < 16 || list_capacity > 4096)
+        return fail(MDG_ERR_INVALID, "list capacity %d not in 16..4096", list_capacity);
+    for (int k = 0; k < 3; ++k)
+        if (s->sys_h[0].Ld[k] < 3.0 * (rf + skin))
+            return fail(MDG_ERR_INVALID, "box edge %g A below 3 (rf + skin)", s->sys_h[0].Ld[k]);
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    const int was_on = s->ls ? s->ls->enabled : 0, k = s->ls ? s->ls->k : 4;
+    const float thr = s->ls ? s->ls->threshold : 1e-3f;
+    const int tc = s->ls ? s->ls->use_tc : 1;
+    rc = ls_configure(s, (float)rf, (float)skin, list_capacity);
+    if (rc) return fail(rc, "learned slow force: allocation failed");
+    s->ls->enabled = was_on;
+    s->ls->k = k;
+    s->ls->threshold = thr;
+    s->ls->use_tc = tc;
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+static int ls_check(mdg_system *s) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (!s->ls) return fail(MDG_ERR_STATE, "learned slow force not configured");
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_num_params(int32_t *n) {
+    if (!n) return fail(MDG_ERR_INVALID, "null argument");
+    *n = kLsParams;
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_set_params(mdg_system *s, const float *params, int32_t n) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (!params || n != kLsParams) return fail(MDG_ERR_INVALID, "expected %d parameters", kLsParams);
+    for (int k = 0; k < n; ++k)
+        if (!std::isfinite(params[k])) return fail(MDG_ERR_INVALID, "parameter %d not finite", k);
+    CK(cudaMemcpyAsync(s->ls->params, params, sizeof(float) * n, cudaMemcpyHostToDevice, s->stream),
+       "copy");
+    CK(cudaMemsetAsync(s->ls->adam_m, 0, sizeof(float) * kLsParams, s->stream), "memset");
+    CK(cudaMemsetAsync(s->ls->adam_v, 0, sizeof(float) * kLsParams, s->stream), "memset");
+    CK(ls_refresh_weights(s), "weights");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    s->ls->trained = 1;
+    s->forces_valid = 0;
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_get_params(mdg_system *s, float *params, int32_t n) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (!params || n != kLsParams) return fail(MDG_ERR_INVALID, "expected %d parameters", kLsParams);
+    CK(cudaMemcpyAsync(params, s->ls->params, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream),
+       "copy");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_frame(mdg_system *s, int32_t slot) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (slot != 0 && slot != 1) return fail(MDG_ERR_INVALID, "slot %d not 0 or 1", slot);
+    const unsigned mask = MDG_MASK(MDG_TERM_COUL_RECIP);
+    rc = ready_for_forces(s, mask);
+    if (rc) return rc;
+    if (!s->pme.on) return fail(MDG_ERR_STATE, "PME has not been configured");
+    s->ls_slot = slot;
+    s->ls_phase = kLsFrame;
+    s->slow_target = s->ls->fs;
+    s->recip_weight = 1.0f;
+    rc = evaluate(s, mask, 0);
+    s->ls_phase = kLsOff;
+    s->slow_target = nullptr;
+    s->forces_valid = 0;  // f now holds no complete force
+    if (rc) return rc;
+    return read_status(s);
+}
+
+MDG_API int mdg_learned_frame_data(mdg_system *s, int32_t slot, float *features, float *vectors,
+                                   float *slow_force, float *predicted) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (slot != 0 && slot != 1) return fail(MDG_ERR_INVALID, "slot %d not 0 or 1", slot);
+    const Learned &L = *s->ls;
+    const size_t n = s->n;
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    if (features)
+        CK(cudaMemcpy(features, L.xraw[slot], sizeof(float) * n * kLsFeat, cudaMemcpyDeviceToHost),
+           "copy");
+    if (vectors || slow_force || predicted) {
+        std::vector<float> buf;
+        if (vectors)
+            CK(cudaMemcpy(vectors, L.S[slot], sizeof(float) * 3 * kLsVec * n, cudaMemcpyDeviceToHost),
+               "copy");
+        if (slow_force) {
+            buf.resize(3 * n);
+            CK(cudaMemcpy(buf.data(), L.T[slot], sizeof(float) * 3 * n, cudaMemcpyDeviceToHost), "copy");
+            for (size_t i = 0; i < n; ++i)
+                for (int d = 0; d < 3; ++d) slow_force[3 * i + d] = buf[(size_t)d * n + i];
+        }
+        if (predicted) {
+            buf.resize((size_t)3 * L.n_rows);
+            CK(cudaMemcpy(buf.data(), L.G[slot], sizeof(float) * buf.size(), cudaMemcpyDeviceToHost),
+               "copy");
+            for (size_t i = 0; i < n; ++i)
+                for (int d = 0; d < 3; ++d) predicted[3 * i + d] = buf[(size_t)d * L.n_rows + i];
+        }
+    }
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_predict(mdg_system *s, int32_t slot, float *predicted) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (slot != 0 && slot != 1) return fail(MDG_ERR_INVALID, "slot %d not 0 or 1", slot);
+    CK(ls_predict(s, slot), "learned prediction");
+    rc = read_status(s);
+    if (rc) return rc;
+    return predicted ? mdg_learned_frame_data(s, slot, nullptr, nullptr, nullptr, predicted)
+                     : MDG_OK;
+}
+
+MDG_API int mdg_learned_train_step(mdg_system *s, float lr, int32_t t, double *loss) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (!(lr > 0.f) || t < 1) return fail(MDG_ERR_INVALID, "lr must be > 0 and t >= 1");
+    CK(ls_train(s, lr, t, loss), "train step");
+    s->ls->trained = 1;
+    return read_status(s);
+}
+
+MDG_API int mdg_set_mts_learned(mdg_system *s, int32_t k, double threshold) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (k == 0 || k == 1) {
+        if (s->ls) s->ls->enabled = 0;
+        s->mts_k = 1;
+    } else {
+        rc = ls_check(s);
+        if (rc) return rc;
+        if (k < 2 || k > 16) return fail(MDG_ERR_INVALID, "outer step %d not in 2..16", k);
+        if (!(threshold > 0.0)) return fail(MDG_ERR_INVALID, "threshold must be positive");
+        if (!s->pme.on) return fail(MDG_ERR_STATE, "PME has not been configured");
+        s->ls->enabled = 1;
+        s->ls->k = k;
+        s->ls->threshold = (float)threshold;
+        s->mts_k = k;
+        CK(cudaMemsetAsync(s->ls->mode, 0, sizeof(int) * 2, s->stream), "memset");
+    }
+    s->forces_valid = 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_set_kernel(mdg_system *s, int32_t tensor_cores) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    s->ls->use_tc = tensor_cores ? 1 : 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_stats(mdg_system *s, double *out8) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (!out8) return fail(MDG_ERR_INVALID, "null argument");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
+    CK(cudaMemcpy(out8, s->ls->stats, sizeof(double) * 8, cudaMemcpyDeviceToHost), "copy");
+    int mode[2] = {0, 0};
+    CK(cudaMemcpy(mode, s->ls->mode, sizeof(mode), cudaMemcpyDeviceToHost), "copy");
+    out8[7] = mode[0];
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_reset_stats(mdg_system *s) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(s->ls->stats, 0, sizeof(double) * 5, s->stream), "memset");
+    CK(cudaStreamSynchronize(s->stream), "synchronize");
     return MDG_OK;
 }
 
@@ -1392,10 +1627,15 @@ MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_en
         if (g.exec && g.mask != mask) drop_graph(s);
     // the force buffer the first pre-force update uses: multiple time steps
     // want the weight of the evaluation that ended the previous step
-    const float want_w = s->step == 0 ? mts_weight(s, (uint64_t)s->mts_k - 1)
-                                      : mts_weight(s, s->step - 1);
+    const float want_w = ls_active(s) ? -1.0f
+                         : s->step == 0 ? mts_weight(s, (uint64_t)s->mts_k - 1)
+                                        : mts_weight(s, s->step - 1);
     if (!s->forces_valid || s->forces_mask != mask || s->forces_weight != want_w) {
-        if (s->mts_k > 1) {
+        if (ls_active(s)) {
+            // learned form: a full evaluation anchors the prediction
+            rc = ls_evaluate(s, mask, 0, kLsAnchor);
+            if (rc) return rc;
+        } else if (s->mts_k > 1) {
             s->recip_weight = want_w;
             rc = evaluate(s, mask, 0);
             s->recip_weight = 1.0f;
@@ -1438,7 +1678,7 @@ MDG_API int mdg_integrate(mdg_system *s, int n_steps, unsigned mask, int want_en
             s->launches += g.steps;
             s->need_reorder = 0;
             s->steps_since_reorder = chunk_start ? 1 : s->steps_since_reorder + 1;
-            s->forces_weight = mts_weight(s, s->step);
+            s->forces_weight = ls_active(s) ? -1.0f : mts_weight(s, s->step);
             s->step += 1;
             remaining -= 1;
         } else if (chunk_start && usable >= R && R >= 2) {

@@ -269,6 +269,85 @@ struct Graph {
     unsigned mask = 0;
 };
 
+// ---- learned slow force (multiple time steps) ------------------------------
+// Per atom i: 64 invariant features (32 cubic B-spline radial bins, channels
+// sum_j q_j phi_b(r_ij) and sum_j phi_b(r_ij), j within rf), a BF16 MLP
+// 64 -> 128 -> 128 -> 16 (SiLU, FP32 accumulation) giving coefficients C_ib
+// on 16 vector basis functions S_ib = q_i sum_j q_j psi_b(r_ij) d_ij / rf^2,
+// and the predicted slow force G_i = sum_b C_ib S_ib (rotation equivariant).
+constexpr int kLsBins = 32;
+constexpr int kLsFeat = 2 * kLsBins;
+constexpr int kLsVec = 16;
+constexpr int kLsHidden = 128;
+constexpr int kLsTile = 128;  // atoms per MLP tile
+// the parameter vector (FP32): feature shift and inverse scale, the three
+// layers (weights stored [in][out]), the output scale
+constexpr int kLsMu = 0;
+constexpr int kLsSig = kLsMu + kLsFeat;
+constexpr int kLsW1 = kLsSig + kLsFeat;
+constexpr int kLsB1 = kLsW1 + kLsFeat * kLsHidden;
+constexpr int kLsW2 = kLsB1 + kLsHidden;
+constexpr int kLsB2 = kLsW2 + kLsHidden * kLsHidden;
+constexpr int kLsW3 = kLsB2 + kLsHidden;
+constexpr int kLsB3 = kLsW3 + kLsHidden * kLsVec;
+constexpr int kLsScale = kLsB3 + kLsVec;
+constexpr int kLsParams = kLsScale + 1;
+// BF16 weight copies: W1, W2, W3 in [in][out] order, then the same three in
+// the tensor-core operand layout (see mdg_learned_tc.cu)
+constexpr int kLsWb = kLsFeat * kLsHidden + kLsHidden * kLsHidden + kLsHidden * kLsVec;
+
+// element (r, k) of a K-major BF16 operand with R rows (R, K multiples of
+// 8), as the tensor cores read it from shared memory without swizzle: 8 x 8
+// core matrices of 128 contiguous bytes, K-chunk-major
+__host__ __device__ constexpr int ls_tc_off(int r, int k, int R) {
+    return ((k >> 3) * (R >> 3) + (r >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
+// features of atom row i inside the tile-major feature array
+__host__ __device__ constexpr size_t ls_xoff(int i, int k) {
+    return (size_t)(i / kLsTile) * kLsTile * kLsFeat + ls_tc_off(i % kLsTile, k, kLsTile);
+}
+
+enum LsPhase { kLsOff = 0, kLsInner = 1, kLsOuter = 2, kLsAnchor = 3, kLsFrame = 4 };
+enum LsMode { kLsLearned = 0, kLsImpulse = 1 };
+
+struct Learned {
+    int configured = 0, enabled = 0, trained = 0;
+    int k = 4;                 // outer step
+    float threshold = 1e-3f;   // judge: relative force error that switches to the fallback
+    float rf = 6.0f, skin = 1.0f;
+    int cap = 256;             // neighbour list entries per atom
+    int nc[3] = {0, 0, 0}, n_cells = 0;
+    int n_rows = 0, n_tiles = 0;  // MLP rows (atoms padded to whole tiles)
+    int use_tc = 1;            // tensor-core (tcgen05) inference kernel (0: SIMT)
+    int *cell_of = nullptr, *cell_count = nullptr, *cell_start = nullptr,
+        *cell_cursor = nullptr, *cell_atoms = nullptr;
+    int *nlist = nullptr, *list = nullptr;  // per slot of the cell order; list: [cap][n]
+    float4 *pos = nullptr;     // wrapped FP32 positions, q sqrt(k_e) (atom order)
+    float4 *cpos = nullptr;    // the same in cell order (list build)
+    float4 *xref = nullptr;    // positions at the last list build (motion test)
+    int *flag = nullptr;       // [0]: rebuild requested, [1]: rebuilding now
+    float *xraw[2] = {nullptr, nullptr};  // raw features of training frames (n x 64)
+    uint16_t *xb[2] = {nullptr, nullptr};  // normalised BF16 features, tiles (ls_xoff)
+    float *S[2] = {nullptr, nullptr};      // vector basis [rows][48] (3 b + axis)
+    float *G[2] = {nullptr, nullptr};      // predicted slow force [3][rows]
+    float *Z1[2] = {nullptr, nullptr}, *Z2[2] = {nullptr, nullptr};  // training
+    float *T[2] = {nullptr, nullptr};      // slow-force targets [3][n]
+    float *params = nullptr;   // FP32 master
+    uint16_t *wb = nullptr;    // BF16 copies (2 * kLsWb)
+    float *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr;
+    float *dout = nullptr;     // [2][rows][16] training gradients at the outputs
+    float *gpart = nullptr;    // per-CTA gradient partials
+    int n_gpart = 0;
+    double *red = nullptr;     // reduction partials
+    int n_red = 0;
+    long long *base = nullptr; // F_slow(t0) - G(t0), fixed point [3][n]
+    unsigned long long *fs = nullptr;  // slow force of an outer step (sorted, fixed point)
+    int *mode = nullptr;       // LsMode of the current interval
+    double *stats = nullptr;   // last error, max error, sum of errors, judged, fallbacks,
+                               // last loss, last target norm
+    int *done = nullptr;       // block counter of the judge's last-block reduction
+};
+
 }  // namespace mdg
 
 struct mdg_system {
@@ -356,6 +435,13 @@ struct mdg_system {
     int mts_k = 1;
     float recip_weight = 1.0f;        // weight of the reciprocal force in the next evaluation
     float forces_weight = 1.0f;       // weight in the force buffer's evaluation
+                                      // (-1: forces of the learned slow-force form)
+    // learned slow force: what the next evaluation does for it (mdg::LsPhase),
+    // and where PME and the excluded-pair correction put their forces (null: f)
+    mdg::Learned *ls = nullptr;
+    int ls_phase = 0;
+    int ls_slot = 0;
+    unsigned long long *slow_target = nullptr;
 
     // nonbonded configuration
     float cutoff = 12.0f, rswitch = 0.0f;
@@ -424,4 +510,14 @@ int upload_sys_table(mdg_system *s);
 void pme_free(mdg_system *s);
 cudaError_t noalloc_scratch(int device, long long **out);  // static scratch of the no-alloc path
 cudaError_t launch_kinetic_scratch(mdg_system *s, long long *acc);
+// learned slow force (mdg_learned.cu)
+int ls_configure(mdg_system *s, float rf, float skin, int cap);
+void ls_free(mdg_system *s);
+cudaError_t ls_side(mdg_system *s, int phase);   // side stream: features, MLP, forces
+cudaError_t ls_after_join(mdg_system *s, int phase);  // main stream: judge, combine, targets
+cudaError_t ls_refresh_weights(mdg_system *s);
+cudaError_t ls_train(mdg_system *s, float lr, int t, double *loss);
+cudaError_t ls_predict(mdg_system *s, int slot);
+cudaError_t ls_mlp_tc(mdg_system *s, int slot, int apply);  // mdg_learned_tc.cu
+int ls_tc_prepare(mdg_system *s);
 }  // namespace mdg

@@ -124,6 +124,7 @@ struct SpArgs {
     int do_excl, do_lj14, do_coul14;
     float excl_weight;  // weight of the excluded-pair reciprocal correction's force
     unsigned long long *f;
+    unsigned long long *fx;  // where the excluded-pair correction's force goes
     long long *energy;
     int *dump;
     long long dump_cap;
@@ -197,12 +198,13 @@ __global__ void k_special(SpArgs a) {
         }
         if (!DUMP && fr != 0.f) {
             const int ki = a.inv_perm[i], kj = a.inv_perm[j];
-            fix_red(&a.f[kj], to_fix(fr * d[0]));
-            fix_red(&a.f[a.n_pad + kj], to_fix(fr * d[1]));
-            fix_red(&a.f[2 * a.n_pad + kj], to_fix(fr * d[2]));
-            fix_red(&a.f[ki], to_fix(-fr * d[0]));
-            fix_red(&a.f[a.n_pad + ki], to_fix(-fr * d[1]));
-            fix_red(&a.f[2 * a.n_pad + ki], to_fix(-fr * d[2]));
+            unsigned long long *ff = is14 ? a.f : a.fx;
+            fix_red(&ff[kj], to_fix(fr * d[0]));
+            fix_red(&ff[a.n_pad + kj], to_fix(fr * d[1]));
+            fix_red(&ff[2 * a.n_pad + kj], to_fix(fr * d[2]));
+            fix_red(&ff[ki], to_fix(-fr * d[0]));
+            fix_red(&ff[a.n_pad + ki], to_fix(-fr * d[1]));
+            fix_red(&ff[2 * a.n_pad + ki], to_fix(-fr * d[2]));
         }
     }
     if (DUMP) return;
@@ -312,6 +314,7 @@ cudaError_t launch_special(mdg_system *s, unsigned mask, int energy, int dump) {
     a.do_lj14 = (mask & MDG_MASK(MDG_TERM_LJ)) && s->lj_on;
     a.do_coul14 = (mask & MDG_MASK(MDG_TERM_COUL_REAL)) && s->coul_mode == MDG_COUL_EWALD;
     a.f = s->f;
+    a.fx = s->slow_target ? s->slow_target : s->f;
     a.energy = s->energy;
     a.dump = s->dump_buf;
     a.dump_cap = s->dump_cap;

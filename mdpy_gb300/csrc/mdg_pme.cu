@@ -550,7 +550,7 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
     a.n_pad = s->n_pad;
     a.grid_i = (unsigned long long *)p.grid_i;
     a.phi = p.grid_r;
-    a.f = s->f;
+    a.f = s->slow_target ? s->slow_target : s->f;  // the learned form's outer steps: apart
     a.tile_spread = s->pme_tiles & 1;
     a.tile_gather = (s->pme_tiles >> 1) & 1;
     a.weight = s->recip_weight;

@@ -22,19 +22,26 @@ from . import unit
 
 class Integrator:
     """``reciprocal_every`` = k > 1: the PME force enters every k-th step with
-    weight k (impulse multiple-time-step scheme, outer step k dt)."""
+    weight k (impulse multiple-time-step scheme, outer step k dt).
+    ``learned`` = a trained :class:`mdpy_gb300.learned.LearnedSlowForce`:
+    full PME every ``learned.outer_step`` steps and the learned prediction of
+    the slow force in between (``reciprocal_every`` is then ignored)."""
     _kind = None
 
-    def __init__(self, time_step, reciprocal_every=1):
+    def __init__(self, time_step, reciprocal_every=1, learned=None):
         self._time_step = float(unit.check_quantity_value(time_step, "femtosecond"))
         self.reciprocal_every = int(reciprocal_every)
+        self.learned = learned
 
     def _configure(self, ensemble):
         raise NotImplementedError
 
     def integrate(self, ensemble, num_steps: int = 1):
         self._configure(ensemble)
-        ensemble.system.set_mts(self.reciprocal_every)
+        if self.learned is not None:
+            self.learned.enable(ensemble.system)
+        else:
+            ensemble.system.set_mts(self.reciprocal_every)
         ensemble.system.integrate(int(num_steps), ensemble.term_mask, want_energy=True)
         ensemble._after_integrate()
 
@@ -56,8 +63,8 @@ class Integrator:
 
 
 class VerletIntegrator(Integrator):
-    def __init__(self, time_step, reciprocal_every=1):
-        super().__init__(time_step, reciprocal_every)
+    def __init__(self, time_step, reciprocal_every=1, learned=None):
+        super().__init__(time_step, reciprocal_every, learned)
 
     def _configure(self, ensemble):
         ensemble.system.integrator_config(_lib.INTEGRATOR_VERLET, self._time_step)
@@ -68,8 +75,9 @@ class LangevinIntegrator(Integrator):
     an mdpy Quantity such as ``Quantity(1, 1/picosecond)`` is converted.
     ``seed`` keys the Philox stream; None draws one from the OS."""
 
-    def __init__(self, time_step, temperature, friction_rate, seed=None, reciprocal_every=1):
-        super().__init__(time_step, reciprocal_every)
+    def __init__(self, time_step, temperature, friction_rate, seed=None, reciprocal_every=1,
+                 learned=None):
+        super().__init__(time_step, reciprocal_every, learned)
         self._temperature = float(unit.check_quantity_value(temperature, "kelvin"))
         if hasattr(friction_rate, "convert_to"):
             import importlib

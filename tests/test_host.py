@@ -258,3 +258,60 @@ def test_charmm_forcefield_emits_device_constraints(monkeypatch):
     assert kinds[:2] == [C.ElectrostaticConstraint, C.CharmmNonbondedConstraint]
     with pytest.raises(ValueError):
         forcefield.CharmmForcefield(w.topology, w.pbc_matrix, long_range_solver="EWALD")
+
+
+def test_learned_parameter_layout_matches_library(lib):
+    """The Python offsets of the learned network's parameter vector and the
+    library's count agree (no GPU needed for the count)."""
+    from mdpy_gb300 import learned as Lr
+
+    assert lib.System.learned_num_params() == Lr.N_PARAMS == 27025
+    p = Lr.init_params(np.random.default_rng(0), scale=2.0)
+    u = Lr.unpack(p)
+    assert u["w1"].shape == (64, 128) and u["w3"].shape == (128, 16) and u["scale"] == 2.0
+    assert np.all(u["sig"] == 1.0) and np.all(u["mu"] == 0.0)
+
+
+def test_learned_reference_features_brute_force():
+    """The FP64 feature reference (tests/learned_ref.py) against a direct
+    double loop on a small periodic system: values, rotation invariance of
+    the features and equivariance of the vector basis."""
+    from tests import learned_ref as R
+
+    rng = np.random.default_rng(1)
+    box = np.array([14.0, 14.0, 14.0])
+    pos = rng.uniform(0, 14.0, (60, 3))
+    q = rng.uniform(-1, 1, 60)
+    rf = 6.0
+    feat, vec = R.features(pos, q, box, rf)
+    f2 = np.zeros_like(feat)
+    v2 = np.zeros_like(vec)
+    for i in range(60):
+        for j in range(60):
+            if i == j:
+                continue
+            d = pos[i] - pos[j]
+            d -= box * np.round(d / box)
+            r = np.linalg.norm(d)
+            if r >= rf:
+                continue
+            for b in range(32):
+                w = R.bspline3(np.array([r / (rf / 33) - b]))[0]
+                f2[i, b] += q[j] * w
+                f2[i, 32 + b] += w
+            for b in range(16):
+                w = R.bspline3(np.array([r / (rf / 17) - b]))[0]
+                v2[i, b] += q[i] * q[j] * w * d / rf ** 2
+    assert np.allclose(feat, f2, atol=1e-12) and np.allclose(vec, v2, atol=1e-12)
+    # basis functions vanish smoothly at rf
+    assert R.bspline3(np.array([rf / (rf / 33) - 31]))[0] == 0.0
+    # rotation of a cluster far from the box edges: invariant features,
+    # rotated vectors
+    big = np.array([100.0, 100.0, 100.0])
+    c = rng.uniform(-4, 4, (30, 3))
+    th = 0.7
+    rot = np.array([[np.cos(th), -np.sin(th), 0], [np.sin(th), np.cos(th), 0], [0, 0, 1]])
+    fa, va = R.features(c + 50.0, q[:30], big, rf)
+    fb, vb = R.features(c @ rot.T + 50.0, q[:30], big, rf)
+    assert np.allclose(fa, fb, atol=1e-10)
+    assert np.allclose(np.einsum("ab,nkb->nka", rot, va), vb, atol=1e-10)
