@@ -63,7 +63,7 @@ def parse():
                         "comma separated; empty: none)")
     p.add_argument("--learned-iters", type=int, default=400,
                    help="training iterations (frame pairs) of each learned form")
-    p.add_argument("--learned-threshold", type=float, default=5e-3,
+    p.add_argument("--learned-threshold", type=float, default=0.05,
                    help="judge threshold of the learned forms (RMS slow-force error over RMS "
                         "total force) above which an interval falls back to the impulse scheme")
     p.add_argument("--no-autotune", action="store_true",

@@ -260,7 +260,8 @@ MDG_API int mdg_set_mts(mdg_system *sys, int k);
  * The multiple-time-step form with a learned prediction between full PME
  * evaluations.  The slow force (PME plus the excluded-pair correction) is
  * computed in full at every k-th step; in between it is predicted as
- * F_slow(t0) + G(x(t)) - G(x(t0)), t0 the last full evaluation, where G is a
+ * F_slow(t0) + J (x(t) - x(t0)) + G(x(t)) - G(x(t0)), t0 the last full
+ * evaluation, J the field-gradient term (mdg_learned_set_terms) and G a
  * rotation-equivariant network: per atom 64 invariant radial features of the
  * neighbours within rf (sum_j q_j phi_b(r_ij) and sum_j phi_b(r_ij) over 32
  * cubic B-spline bins), a BF16 MLP 64-128-128-16 (SiLU, FP32 accumulation)
@@ -298,6 +299,16 @@ MDG_API int mdg_learned_predict(mdg_system *sys, int32_t slot, float *predicted)
 /* k >= 2: use the learned form with outer step k and judge threshold;
  * k = 0 or 1: off (and the impulse scheme off).  mdg_set_mts turns it off. */
 MDG_API int mdg_set_mts_learned(mdg_system *sys, int32_t k, double threshold);
+/* Terms of the prediction between full evaluations (default: the network
+ * alone -- on flexible water the field-gradient term removes only ~4 % of
+ * the held force's error at k = 4: the slow force changes mostly through
+ * the motion of the other atoms):
+ * field_gradient: J_i (x_i(t) - x_i(t0)) with J_i = d F_slow,i / d x_i at t0
+ * (the other atoms held), from the B-spline second derivatives of the PME
+ * potential (order 4) less the atom's own smeared charge and its excluded
+ * partners; network: G(x(t)) - G(x(t0)), trained on what the first term
+ * leaves.  Both off: the slow force of t0 is held. */
+MDG_API int mdg_learned_set_terms(mdg_system *sys, int32_t field_gradient, int32_t network);
 /* 1: the tcgen05 tensor-core MLP kernel for inference; 0: the SIMT kernel */
 MDG_API int mdg_learned_set_kernel(mdg_system *sys, int32_t tensor_cores);
 /* out[8]: last judged error, largest, sum of errors, judgements, fallbacks,

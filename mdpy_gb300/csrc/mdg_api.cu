@@ -598,9 +598,12 @@ MDG_API int mdg_system_set_boxes(mdg_system *s, const double *boxes) {
     if (s->ls) {  // the learned form's cell grid follows the box (parameters kept)
         const Learned &L = *s->ls;
         const int on = L.enabled, k = L.k, tc = L.use_tc, cap = L.cap;
+        const int ty = L.use_taylor, nt = L.use_net;
         const float thr = L.threshold, rf = L.rf, skin = L.skin;
         rc = ls_configure(s, rf, skin, cap);
         if (rc) return fail(rc, "learned slow force: box too small or allocation failed");
+        s->ls->use_taylor = ty;
+        s->ls->use_net = nt;
         s->ls->enabled = on;
         s->ls->k = k;
         s->ls->threshold = thr;
@@ -1399,8 +1402,11 @@ MDG_API int mdg_learned_config(mdg_system *s, double rf, double skin, int list_c
     const int was_on = s->ls ? s->ls->enabled : 0, k = s->ls ? s->ls->k : 4;
     const float thr = s->ls ? s->ls->threshold : 1e-3f;
     const int tc = s->ls ? s->ls->use_tc : 1;
+    const int ty = s->ls ? s->ls->use_taylor : 0, nt = s->ls ? s->ls->use_net : 1;
     rc = ls_configure(s, (float)rf, (float)skin, list_capacity);
     if (rc) return fail(rc, "learned slow force: allocation failed");
+    s->ls->use_taylor = ty;
+    s->ls->use_net = nt;
     s->ls->enabled = was_on;
     s->ls->k = k;
     s->ls->threshold = thr;
@@ -1550,6 +1556,16 @@ MDG_API int mdg_learned_set_kernel(mdg_system *s, int32_t tensor_cores) {
     int rc = ls_check(s);
     if (rc) return rc;
     s->ls->use_tc = tensor_cores ? 1 : 0;
+    drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_set_terms(mdg_system *s, int32_t field_gradient, int32_t network) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    s->ls->use_taylor = field_gradient ? 1 : 0;
+    s->ls->use_net = network ? 1 : 0;
+    s->forces_valid = 0;
     drop_graph(s);
     return MDG_OK;
 }

@@ -319,12 +319,15 @@ struct Learned {
     int nc[3] = {0, 0, 0}, n_cells = 0;
     int n_rows = 0, n_tiles = 0;  // MLP rows (atoms padded to whole tiles)
     int use_tc = 1;            // tensor-core (tcgen05) inference kernel (0: SIMT)
+    int use_taylor = 0;        // field-gradient term J (x - x0) in the prediction
+    int use_net = 1;           // the network's G(x) - G(x0) in the prediction
     int *cell_of = nullptr, *cell_count = nullptr, *cell_start = nullptr,
         *cell_cursor = nullptr, *cell_atoms = nullptr;
     int *nlist = nullptr, *list = nullptr;  // per slot of the cell order; list: [cap][n]
     float4 *pos = nullptr;     // wrapped FP32 positions, q sqrt(k_e) (atom order)
     float4 *cpos = nullptr;    // the same in cell order (list build)
     float4 *xref = nullptr;    // positions at the last list build (motion test)
+    int *slot_of = nullptr;    // atom -> its slot in the cell order of the last build
     int *flag = nullptr;       // [0]: rebuild requested, [1]: rebuilding now
     float *xraw[2] = {nullptr, nullptr};  // raw features of training frames (n x 64)
     uint16_t *xb[2] = {nullptr, nullptr};  // normalised BF16 features, tiles (ls_xoff)
@@ -341,6 +344,10 @@ struct Learned {
     double *red = nullptr;     // reduction partials
     int n_red = 0;
     long long *base = nullptr; // F_slow(t0) - G(t0), fixed point [3][n]
+    long long *J = nullptr;    // d F_slow / d x_i at t0 (xx, yy, zz, xy, xz, yz), fixed [6][n]
+    long long *Jn = nullptr;   // the same at the current full evaluation
+    float4 *x0 = nullptr;      // positions at t0
+    float4 *fpos[2] = {nullptr, nullptr};  // positions of the training frames
     unsigned long long *fs = nullptr;  // slow force of an outer step (sorted, fixed point)
     int *mode = nullptr;       // LsMode of the current interval
     double *stats = nullptr;   // last error, max error, sum of errors, judged, fallbacks,

@@ -73,6 +73,11 @@ struct Geo {
     float L[3], invL[3], ncl[3];  // box, inverse, cells per A
     double Ld[3], invLd[3];
     float rf2, rl2, half_skin2, inv_h1, inv_h2, s_scale;
+    // PME potential grid of the system (order 4) for the field-gradient term
+    const float *phi;
+    int K[3];
+    float kl[3];
+    float beta, self_h;  // Ewald beta; 4 beta^3 / (3 sqrt(pi))
 };
 
 // Wrapped FP32 positions of every atom; raises the rebuild flag when an
@@ -92,6 +97,7 @@ __global__ void __launch_bounds__(256) k_ls_pos(const double *__restrict__ x,
             p[d] = v;
         }
         L.pos[i] = make_float4(p[0], p[1], p[2], q[i]);
+        L.cpos[L.slot_of[i]] = make_float4(p[0], p[1], p[2], q[i]);
         const float4 r = L.xref[i];
         float d0 = p[0] - r.x, d1 = p[1] - r.y, d2 = p[2] - r.z;
         d0 -= g.L[0] * rintf(d0 * g.invL[0]);
@@ -216,7 +222,9 @@ __global__ void __launch_bounds__(256) k_ls_cellsort(Learned L) {
 }
 
 // Neighbour list of slot s (cell order: a warp's atoms share most of their
-// 27 cells, read from the cell-ordered positions), entries list[e][s].
+// 27 cells, read from the cell-ordered positions), entries list[e][s] are
+// slots too, so the feature kernel reads its neighbours from the
+// cell-ordered copy that k_ls_pos refreshes every step.
 // 1-2 / 1-3 partners (the reciprocal sum and the excluded-pair correction
 // cancel for them, so they carry no slow force) are left out.  Stores the
 // build positions for the motion test.
@@ -230,6 +238,7 @@ __global__ void __launch_bounds__(128) k_ls_list(Learned L, Geo g, const int *__
     const int i = L.cell_atoms[s0];
     const float4 pi = L.cpos[s0];
     L.xref[i] = pi;
+    L.slot_of[i] = s0;
     int pr[kMaxPw];
 #pragma unroll
     for (int u = 0; u < kMaxPw; ++u) pr[u] = u < pw ? partners[(size_t)i * pw + u] : -1;
@@ -246,20 +255,20 @@ __global__ void __launch_bounds__(128) k_ls_list(Learned L, Geo g, const int *__
                 const int st = L.cell_start[cell], en = L.cell_start[cell + 1];
 #pragma unroll 4
                 for (int q = st; q < en; ++q) {
-                    const float4 pj = L.cpos[q];
+                    const float4 pj = __ldg(&L.cpos[q]);
                     float d0 = pi.x - pj.x, d1 = pi.y - pj.y, d2 = pi.z - pj.z;
                     d0 -= g.L[0] * rintf(d0 * g.invL[0]);
                     d1 -= g.L[1] * rintf(d1 * g.invL[1]);
                     d2 -= g.L[2] * rintf(d2 * g.invL[2]);
                     if (d0 * d0 + d1 * d1 + d2 * d2 >= g.rl2) continue;
-                    const int j = L.cell_atoms[q];
+                    const int j = __ldg(&L.cell_atoms[q]);
                     if (j == i) continue;
                     bool excluded = false;
 #pragma unroll
                     for (int u = 0; u < kMaxPw; ++u) excluded |= pr[u] == j;
                     for (int u = kMaxPw; u < pw; ++u) excluded |= partners[(size_t)i * pw + u] == j;
                     if (excluded) continue;
-                    if (cnt < L.cap) L.list[(size_t)cnt * g.n + s0] = j;
+                    if (cnt < L.cap) L.list[(size_t)cnt * g.n + s0] = q;
                     ++cnt;
                 }
             }
@@ -292,16 +301,20 @@ __global__ void __launch_bounds__(kFeatThreads) k_ls_features(Learned L, Geo g, 
     for (int b = 0; b < kAccP; ++b) a[b * kFeatThreads] = 0.f;
     if (s0 >= g.n) return;  // no block barrier in this kernel
     const int i = L.cell_atoms[s0];
-    const float4 pi = L.pos[i];
+    const float4 pi = L.cpos[s0];
     const int cnt = L.nlist[s0];
-    int j = cnt > 0 ? L.list[s0] : i;
-    float4 pj = L.pos[j];
-    for (int e = 0; e < cnt; ++e) {
-        const float4 pc = pj;
-        if (e + 1 < cnt) {
-            j = L.list[(size_t)(e + 1) * g.n + s0];
-            pj = L.pos[j];
+    constexpr int kB = 8;  // entries whose loads are in flight together
+    for (int e0 = 0; e0 < cnt; e0 += kB) {
+        float4 pb[kB];
+#pragma unroll
+        for (int m = 0; m < kB; ++m) {
+            const int jj = e0 + m < cnt ? __ldg(&L.list[(size_t)(e0 + m) * g.n + s0]) : s0;
+            pb[m] = __ldg(&L.cpos[jj]);
         }
+#pragma unroll
+        for (int m = 0; m < kB; ++m) {
+        if (e0 + m >= cnt) break;
+        const float4 pc = pb[m];
         float d0 = pi.x - pc.x, d1 = pi.y - pc.y, d2 = pi.z - pc.z;
         d0 -= g.L[0] * rintf(d0 * g.invL[0]);
         d1 -= g.L[1] * rintf(d1 * g.invL[1]);
@@ -341,22 +354,33 @@ __global__ void __launch_bounds__(kFeatThreads) k_ls_features(Learned L, Geo g, 
         }
 #pragma unroll
         for (int m = 0; m < 12; ++m) fv[m * kFeatThreads] = vv[m];
+        }
     }
-    // features (bins 0..31 sit in padded slots 1..32): normalised, BF16, tile layout
-#pragma unroll 4
-    for (int k = 0; k < kLsFeat; k += 2) {
-        const int p0 = (k < kLsBins ? k : kFB + k - kLsBins) + 1;
-        const float r0 = a[p0 * kFeatThreads], r1 = a[(p0 + 1) * kFeatThreads];
-        if (RAW) *(float2 *)(L.xraw[slot] + (size_t)i * kLsFeat + k) = make_float2(r0, r1);
-        const float n0 = (r0 - L.params[kLsMu + k]) * L.params[kLsSig + k];
-        const float n1 = (r1 - L.params[kLsMu + k + 1]) * L.params[kLsSig + k + 1];
-        *(unsigned *)(L.xb[slot] + ls_xoff(i, k)) =
-            (unsigned)to_bf(n0) | ((unsigned)to_bf(n1) << 16);
+    // features (bins 0..31 sit in padded slots 1..32): normalised, BF16, tile
+    // layout, 8 features (one 16-byte core-matrix row) per store
+#pragma unroll 1
+    for (int k0 = 0; k0 < kLsFeat; k0 += 8) {
+        unsigned h[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = k0 + 2 * u;
+            const int p0 = (k < kLsBins ? k : kFB + k - kLsBins) + 1;
+            const float r0 = a[p0 * kFeatThreads], r1 = a[(p0 + 1) * kFeatThreads];
+            if (RAW) *(float2 *)(L.xraw[slot] + (size_t)i * kLsFeat + k) = make_float2(r0, r1);
+            const float n0 = (r0 - L.params[kLsMu + k]) * L.params[kLsSig + k];
+            const float n1 = (r1 - L.params[kLsMu + k + 1]) * L.params[kLsSig + k + 1];
+            h[u] = (unsigned)to_bf(n0) | ((unsigned)to_bf(n1) << 16);
+        }
+        *(uint4 *)(L.xb[slot] + ls_xoff(i, k0)) = make_uint4(h[0], h[1], h[2], h[3]);
     }
     const float qs = pi.w * g.s_scale;
-    float *so = L.S[slot] + (size_t)i * 3 * kLsVec;
+    float4 *so = (float4 *)(L.S[slot] + (size_t)i * 3 * kLsVec);
 #pragma unroll 4
-    for (int c = 0; c < 3 * kLsVec; ++c) so[c] = a[(2 * kFB + 3 + c) * kFeatThreads] * qs;
+    for (int c = 0; c < 3 * kLsVec; c += 4)
+        so[c / 4] = make_float4(a[(2 * kFB + 3 + c) * kFeatThreads] * qs,
+                                a[(2 * kFB + 4 + c) * kFeatThreads] * qs,
+                                a[(2 * kFB + 5 + c) * kFeatThreads] * qs,
+                                a[(2 * kFB + 6 + c) * kFeatThreads] * qs);
 }
 
 // ---- SIMT MLP ---------------------------------------------------------------
@@ -512,23 +536,165 @@ __device__ void reduce_pairs(const double *red, int n, double &a, double &b) {
     __syncthreads();
 }
 
+// ---- field-gradient (Taylor) term -------------------------------------------
+// J_i = d F_slow,i / d x_i with the other atoms held: -q_i times the Hessian
+// of the reciprocal potential at x_i (order-4 B-spline second derivatives of
+// the PME potential grid), less the atom's own smeared charge (a constant
+// -4 beta^3 / (3 sqrt pi) q_i^2 I in J) and less its excluded partners (added
+// back pair by pair below: their share cancels against the excluded-pair
+// correction).  Then F_slow,i(t) ~ F_slow,i(t0) + J_i (x_i(t) - x_i(t0)).
+__device__ __forceinline__ void bspline4_d2(float w, float (&th)[4], float (&dth)[4],
+                                            float (&ddth)[4]) {
+    // grid point g0 + c carries M4(w + 3 - c) (the PME kernels' indexing)
+    const float w2 = w * w, w3 = w2 * w, u = 1.f - w;
+    th[0] = u * u * u * (1.f / 6.f);
+    th[1] = (3.f * w3 - 6.f * w2 + 4.f) * (1.f / 6.f);
+    th[2] = (-3.f * w3 + 3.f * w2 + 3.f * w + 1.f) * (1.f / 6.f);
+    th[3] = w3 * (1.f / 6.f);
+    dth[0] = -0.5f * u * u;
+    dth[1] = 1.5f * w2 - 2.f * w;
+    dth[2] = -1.5f * w2 + w + 0.5f;
+    dth[3] = 0.5f * w2;
+    ddth[0] = u;
+    ddth[1] = 3.f * w - 2.f;
+    ddth[2] = 1.f - 3.f * w;
+    ddth[3] = w;
+}
+
+__global__ void __launch_bounds__(256) k_ls_hessian(Learned L, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    const float4 p = L.pos[i];
+    float th[3][4], dth[3][4], ddth[3][4];
+    int g0[3];
+    const float xs[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int K = g.K[d];
+        float u = fmodf(xs[d] * g.kl[d], (float)K);
+        if (u < 0.f) u += (float)K;
+        if (!(u >= 0.f && u < (float)K)) u = 0.f;
+        int m = min((int)u, K - 1);
+        const float w = u - (float)m;
+        g0[d] = m - 3;
+        if (g0[d] < 0) g0[d] += K;
+        bspline4_d2(w, th[d], dth[d], ddth[d]);
+    }
+    float h[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // xx yy zz xy xz yz
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const int ga = (g0[0] + a) % g.K[0];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int gb = (g0[1] + b) % g.K[1];
+            const float *row = g.phi + ((size_t)ga * g.K[1] + gb) * g.K[2];
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float v = __ldg(&row[(g0[2] + c) % g.K[2]]);
+                s0 = fmaf(th[2][c], v, s0);
+                s1 = fmaf(dth[2][c], v, s1);
+                s2 = fmaf(ddth[2][c], v, s2);
+            }
+            h[0] = fmaf(ddth[0][a] * th[1][b], s0, h[0]);
+            h[1] = fmaf(th[0][a] * ddth[1][b], s0, h[1]);
+            h[2] = fmaf(th[0][a] * th[1][b], s2, h[2]);
+            h[3] = fmaf(dth[0][a] * dth[1][b], s0, h[3]);
+            h[4] = fmaf(dth[0][a] * th[1][b], s1, h[4]);
+            h[5] = fmaf(th[0][a] * dth[1][b], s1, h[5]);
+        }
+    }
+    const float q = p.w, sh = g.self_h * q * q;
+    const float sc[6] = {g.kl[0] * g.kl[0], g.kl[1] * g.kl[1], g.kl[2] * g.kl[2],
+                         g.kl[0] * g.kl[1], g.kl[0] * g.kl[2], g.kl[1] * g.kl[2]};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const float jv = -q * h[c] * sc[c] - (c < 3 ? sh : 0.f);
+        L.Jn[(size_t)c * g.n + i] = to_fix(jv);
+    }
+}
+
+// + q_i q_j Hess k(r_ij), k(r) = erf(beta r) / r, for each excluded pair
+__global__ void __launch_bounds__(256) k_ls_hessian_excl(Learned L, Geo g,
+                                                         const int2 *__restrict__ excl, int n_excl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_excl) return;
+    const int2 pr = excl[t];
+    const float4 pi = L.pos[pr.x], pj = L.pos[pr.y];
+    float d[3] = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] -= g.L[k] * rintf(d[k] * g.invL[k]);
+    const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (!(r2 > 0.f)) return;
+    const float r = sqrtf(r2), br = g.beta * r;
+    const float ef = erff(br);
+    const float gg = 1.1283791670955126f * g.beta * expf(-br * br);  // 2 beta / sqrt(pi) e^-b2r2
+    const float k1 = gg / r - ef / r2;                                 // k'
+    const float k2 = -2.f * g.beta * g.beta * gg - 2.f * gg / r2 + 2.f * ef / (r2 * r);  // k''
+    const float qq = pi.w * pj.w;
+    const float a = qq * (k2 - k1 / r) / r2, b = qq * k1 / r;  // H = a d d^T + b I
+    const float hv[6] = {a * d[0] * d[0] + b, a * d[1] * d[1] + b, a * d[2] * d[2] + b,
+                         a * d[0] * d[1], a * d[0] * d[2], a * d[1] * d[2]};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const long long v = to_fix(hv[c]);
+        fix_red((unsigned long long *)&L.Jn[(size_t)c * g.n + pr.x], v);
+        fix_red((unsigned long long *)&L.Jn[(size_t)c * g.n + pr.y], v);
+    }
+}
+
+// J (x - x0) with the minimum image, from a fixed-point J
+__device__ __forceinline__ void taylor_term(const long long *J, int n, int i, float4 x, float4 x0,
+                                            const Geo &g, float (&out)[3]) {
+    float d[3] = {x.x - x0.x, x.y - x0.y, x.z - x0.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] -= g.L[k] * rintf(d[k] * g.invL[k]);
+    float j[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) j[c] = (float)((double)J[(size_t)c * n + i] * kFixInv);
+    out[0] = j[0] * d[0] + j[3] * d[1] + j[4] * d[2];
+    out[1] = j[3] * d[0] + j[1] * d[1] + j[5] * d[2];
+    out[2] = j[4] * d[0] + j[5] * d[1] + j[2] * d[2];
+}
+
+// inner step of the learned form: f += base + G + J (x - x0)
+__global__ void __launch_bounds__(256) k_ls_apply(Learned L, Geo g, const int *__restrict__ inv_perm,
+                                                  unsigned long long *__restrict__ f, int taylor,
+                                                  int net) {
+    if (*L.mode != kLsLearned) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    float tt[3] = {0.f, 0.f, 0.f};
+    if (taylor) taylor_term(L.J, g.n, i, L.pos[i], L.x0[i], g, tt);
+    const int k = inv_perm[i];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        long long v = L.base[(size_t)d * g.n + i] + to_fix(tt[d]);
+        if (net) v += to_fix(L.G[0][(size_t)d * g.n_rows + i]);
+        fix_red(&f[(size_t)d * g.n_pad + k], v);
+    }
+}
+
 // ---- judge and combine (outer steps) ----------------------------------------
 // Relative RMS error of the prediction base + G against the slow force just
 // computed, normalised by the total force; the last block reduces the
 // per-block partials in block order and sets the mode of the next interval.
 __global__ void __launch_bounds__(256) k_ls_judge(Learned L, Geo g, const int *__restrict__ inv_perm,
                                                   const unsigned long long *__restrict__ f,
-                                                  int anchor, int *done) {
+                                                  int anchor, int *done, int taylor, int net) {
     __shared__ double s_e[8], s_t[8];
     __shared__ bool last;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double e2 = 0.0, t2 = 0.0;
     if (i < g.n && !anchor) {
         const int k = inv_perm[i];
+        float tt[3] = {0.f, 0.f, 0.f};
+        if (taylor) taylor_term(L.J, g.n, i, L.pos[i], L.x0[i], g, tt);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const long long fs = (long long)L.fs[(size_t)d * g.n_pad + k];
-            const long long pr = L.base[(size_t)d * g.n + i] + to_fix(L.G[0][(size_t)d * g.n_rows + i]);
+            long long pr = L.base[(size_t)d * g.n + i] + to_fix(tt[d]);
+            if (net) pr += to_fix(L.G[0][(size_t)d * g.n_rows + i]);
             const double e = (double)(pr - fs) * kFixInv;
             const double tt = (double)((long long)f[(size_t)d * g.n_pad + k] + fs) * kFixInv;
             e2 += e * e;
@@ -582,7 +748,8 @@ __global__ void __launch_bounds__(256) k_ls_judge(Learned L, Geo g, const int *_
 // the slow force its exact total weight; base = F_slow - G for the interval
 // that starts here.
 __global__ void __launch_bounds__(256) k_ls_combine(Learned L, Geo g, const int *__restrict__ inv_perm,
-                                                    unsigned long long *__restrict__ f, int kout) {
+                                                    unsigned long long *__restrict__ f, int kout,
+                                                    int net) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
     const long long w2 = (L.mode[0] == kLsLearned ? 1 : kout) + (L.mode[1] == kLsLearned ? 1 : kout);
@@ -594,8 +761,11 @@ __global__ void __launch_bounds__(256) k_ls_combine(Learned L, Geo g, const int 
         // half-integer weight rounds the fixed-point word to nearest
         const long long add = (w2 & 1) ? (fs * w2 + (fs >= 0 ? 1 : -1)) / 2 : fs * (w2 / 2);
         f[(size_t)d * g.n_pad + k] += (unsigned long long)add;
-        L.base[(size_t)d * g.n + i] = fs - to_fix(L.G[0][(size_t)d * g.n_rows + i]);
+        L.base[(size_t)d * g.n + i] = fs - (net ? to_fix(L.G[0][(size_t)d * g.n_rows + i]) : 0ll);
     }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) L.J[(size_t)c * g.n + i] = L.Jn[(size_t)c * g.n + i];
+    L.x0[i] = L.pos[i];
 }
 
 // ---- training -----------------------------------------------------------------
@@ -604,6 +774,10 @@ __global__ void __launch_bounds__(256) k_ls_target(Learned L, Geo g, const int *
                                                    int slot) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
+    L.fpos[slot][i] = L.pos[i];
+    if (slot == 0)  // the field-gradient term of the pair's first frame
+#pragma unroll
+        for (int c = 0; c < 6; ++c) L.J[(size_t)c * g.n + i] = L.Jn[(size_t)c * g.n + i];
     const int k = inv_perm[i];
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -611,11 +785,15 @@ __global__ void __launch_bounds__(256) k_ls_target(Learned L, Geo g, const int *
             (float)((double)(long long)L.fs[(size_t)d * g.n_pad + k] * kFixInv);
 }
 
+// the network's target is the slow-force change less the field-gradient
+// term (when that term is in use)
 __device__ __forceinline__ void residual(const Learned &L, const Geo &g, int i, float (&R)[3],
                                          float (&dT)[3]) {
+    float tt[3] = {0.f, 0.f, 0.f};
+    if (L.use_taylor) taylor_term(L.J, g.n, i, L.fpos[1][i], L.fpos[0][i], g, tt);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        dT[d] = L.T[1][(size_t)d * g.n + i] - L.T[0][(size_t)d * g.n + i];
+        dT[d] = L.T[1][(size_t)d * g.n + i] - L.T[0][(size_t)d * g.n + i] - tt[d];
         R[d] = (L.G[1][(size_t)d * g.n_rows + i] - L.G[0][(size_t)d * g.n_rows + i]) - dT[d];
     }
 }
@@ -847,6 +1025,13 @@ Geo make_geo(const mdg_system *s) {
     const float rl = L.rf + L.skin;
     g.rl2 = rl * rl;
     g.half_skin2 = 0.25f * L.skin * L.skin;
+    g.phi = s->pme.grid_r ? s->pme.grid_r + d.grid_off : nullptr;
+    for (int k = 0; k < 3; ++k) {
+        g.K[k] = d.K[k];
+        g.kl[k] = d.kl[k];
+    }
+    g.beta = (float)s->beta;
+    g.self_h = (float)(4.0 * s->beta * s->beta * s->beta / (3.0 * 1.7724538509055159));
     g.inv_h1 = (float)(kLsBins + 1) / L.rf;
     g.inv_h2 = (float)(kLsVec + 1) / L.rf;
     g.s_scale = 1.0f / (L.rf * L.rf);
@@ -915,6 +1100,7 @@ int ls_configure(mdg_system *s, float rf, float skin, int cap) {
     LA(L->pos, n);
     LA(L->cpos, n);
     LA(L->xref, n);
+    LA(L->slot_of, n);
     LA(L->flag, 2);
     for (int q = 0; q < 2; ++q) {
         LA(L->xraw[q], n * kLsFeat);
@@ -933,6 +1119,11 @@ int ls_configure(mdg_system *s, float rf, float skin, int cap) {
     LA(L->gpart, (size_t)L->n_gpart * kLsParams);
     LA(L->red, 2 * (size_t)L->n_red);
     LA(L->base, 3 * n);
+    LA(L->J, 6 * n);
+    LA(L->Jn, 6 * n);
+    LA(L->x0, n);
+    LA(L->fpos[0], n);
+    LA(L->fpos[1], n);
     LA(L->fs, 3 * (size_t)s->n_pad);
     LA(L->mode, 2);
     LA(L->stats, 8);
@@ -980,6 +1171,7 @@ void ls_free(mdg_system *s) {
     ls_dfree(L->pos);
     ls_dfree(L->cpos);
     ls_dfree(L->xref);
+    ls_dfree(L->slot_of);
     ls_dfree(L->flag);
     for (int q = 0; q < 2; ++q) {
         ls_dfree(L->xraw[q]);
@@ -998,6 +1190,11 @@ void ls_free(mdg_system *s) {
     ls_dfree(L->gpart);
     ls_dfree(L->red);
     ls_dfree(L->base);
+    ls_dfree(L->J);
+    ls_dfree(L->Jn);
+    ls_dfree(L->x0);
+    ls_dfree(L->fpos[0]);
+    ls_dfree(L->fpos[1]);
     ls_dfree(L->fs);
     ls_dfree(L->mode);
     ls_dfree(L->stats);
@@ -1036,23 +1233,42 @@ cudaError_t ls_side(mdg_system *s, int phase) {
     k_ls_cellsort<<<(L.n_cells * 32 + 255) / 256, 256, 0, st>>>(L);
     k_ls_list<<<(n + 127) / 128, 128, 0, st>>>(L, g, s->partners, s->pw, s->status);
     s->launches += 7;
-    const int gated = phase == kLsInner ? 1 : 0;
-    const int fb = (n + kFeatThreads - 1) / kFeatThreads;
-    if (phase == kLsFrame) k_ls_features<true><<<fb, kFeatThreads, 0, st>>>(L, g, slot, 0);
-    else k_ls_features<false><<<fb, kFeatThreads, 0, st>>>(L, g, slot, gated);
-    s->launches += 1;
+    const bool full = phase != kLsInner;
+    const bool taylor = L.use_taylor && s->pme.order == 4 && g.phi;
+    if (full && taylor) {  // the field-gradient term at this full evaluation
+        k_ls_hessian<<<nb, tb, 0, st>>>(L, g);
+        s->launches += 1;
+        if (s->n_excl > 0) {
+            k_ls_hessian_excl<<<(s->n_excl + 255) / 256, 256, 0, st>>>(L, g, s->excl_pairs,
+                                                                       s->n_excl);
+            s->launches += 1;
+        }
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    if (phase == kLsFrame) {
-        k_ls_mlp<true, false><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, slot, s->f, s->inv_perm);
+    const bool net = L.use_net || phase == kLsFrame;
+    if (net) {
+        const int gated = phase == kLsInner ? 1 : 0;
+        const int fb = (n + kFeatThreads - 1) / kFeatThreads;
+        if (phase == kLsFrame) k_ls_features<true><<<fb, kFeatThreads, 0, st>>>(L, g, slot, 0);
+        else k_ls_features<false><<<fb, kFeatThreads, 0, st>>>(L, g, slot, gated);
         s->launches += 1;
-        return cudaGetLastError();
+        if (phase == kLsFrame) {
+            k_ls_mlp<true, false><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, slot, s->f, s->inv_perm);
+            s->launches += 1;
+        } else if (L.use_tc) {
+            e = ls_mlp_tc(s, 0, 0);
+        } else {
+            k_ls_mlp<false, false><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, 0, s->f, s->inv_perm);
+            s->launches += 1;
+        }
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
     }
-    const int apply = phase == kLsInner ? 1 : 0;
-    if (L.use_tc) return ls_mlp_tc(s, 0, apply);
-    if (apply) k_ls_mlp<false, true><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, 0, s->f, s->inv_perm);
-    else k_ls_mlp<false, false><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, 0, s->f, s->inv_perm);
-    s->launches += 1;
+    if (phase == kLsInner) {  // the predicted slow force joins the other forces
+        k_ls_apply<<<nb, tb, 0, st>>>(L, g, s->inv_perm, s->f, taylor ? 1 : 0, L.use_net);
+        s->launches += 1;
+    }
     return cudaGetLastError();
 }
 
@@ -1068,9 +1284,10 @@ cudaError_t ls_after_join(mdg_system *s, int phase) {
         return cudaGetLastError();
     }
     if (phase != kLsOuter && phase != kLsAnchor) return cudaSuccess;
+    const int taylor = L.use_taylor && s->pme.order == 4 && g.phi ? 1 : 0;
     k_ls_judge<<<nb, tb, 0, s->stream>>>(L, g, s->inv_perm, s->f, phase == kLsAnchor ? 1 : 0,
-                                         L.done);
-    k_ls_combine<<<nb, tb, 0, s->stream>>>(L, g, s->inv_perm, s->f, s->ls->k);
+                                         L.done, taylor, L.use_net);
+    k_ls_combine<<<nb, tb, 0, s->stream>>>(L, g, s->inv_perm, s->f, s->ls->k, L.use_net);
     s->launches += 2;
     return cudaGetLastError();
 }

@@ -2,9 +2,12 @@
 
 Full PME runs every ``outer_step``-th step.  In between, the slow force
 (reciprocal space plus the excluded-pair correction) is predicted as
-``F_slow(t0) + G(x(t)) - G(x(t0))`` by a small rotation-equivariant network
-G evaluated on the device every step (libmdg: ``mdg_learned_*``; the network
-is described in include/mdg.h).  Each full evaluation judges the prediction;
+``F_slow(t0) + J (x(t) - x(t0)) + G(x(t)) - G(x(t0))``: J is each atom's
+field-gradient matrix from the last PME evaluation (the change of its slow
+force as it moves through the field of the others), and G a small
+rotation-equivariant network evaluated on the device every step, trained on
+what the first term leaves (libmdg: ``mdg_learned_*``; the network is
+described in include/mdg.h).  Each full evaluation judges the prediction;
 above ``threshold`` (RMS error over RMS total force) the next interval falls
 back to the impulse scheme, and the learned form resumes when the judged
 error is back under it.
@@ -69,7 +72,7 @@ class LearnedSlowForce:
     """Configuration, parameters and training of the learned slow force."""
 
     def __init__(self, outer_step=4, threshold=2e-3, rf=6.0, skin=1.0, list_capacity=256,
-                 params=None, tensor_cores=True):
+                 params=None, tensor_cores=True, field_gradient=False, network=True):
         if not 2 <= int(outer_step) <= 16:
             raise ValueError("outer_step must be in 2..16")
         self.outer_step = int(outer_step)
@@ -77,6 +80,7 @@ class LearnedSlowForce:
         self.rf, self.skin, self.list_capacity = float(rf), float(skin), int(list_capacity)
         self.params = None if params is None else np.asarray(params, np.float32).copy()
         self.tensor_cores = bool(tensor_cores)
+        self.field_gradient, self.network = bool(field_gradient), bool(network)
         self.history = []
         self._attached = set()
 
@@ -90,6 +94,7 @@ class LearnedSlowForce:
         if self.params is not None:
             system.learned_set_params(self.params)
         system.learned_set_kernel(self.tensor_cores)
+        system.learned_set_terms(self.field_gradient, self.network)
 
     def enable(self, system):
         self.attach(system)
@@ -106,20 +111,28 @@ class LearnedSlowForce:
         system.learned_frame(1)
 
     def normalise(self, system, mask=_lib.MASK_ALL, seed=0):
-        """Feature shift/scale, output scale and a physical starting point
-        from one frame pair; fresh weights.
+        """Feature shift/scale and output scale from one frame pair; fresh
+        weights.  Also two diagnostics:
 
-        The slow force is a pair sum of the smooth Ewald kernel over all
-        non-excluded pairs, so G with environment-independent coefficients
-        C_b already reproduces the part of its change that comes from pairs
-        within rf.  Those 16 constants are fitted by least squares to the
-        frame pair and become the output biases; the network learns the
-        environment-dependent rest.  ``self.pair_model_loss`` is that fit's
-        relative loss."""
+        ``baseline_loss``: the relative loss of G = 0 on the device's target
+        (the slow-force change less the field-gradient term when that term is
+        on): what the field-gradient term alone leaves of the change.
+
+        ``pair_model_loss``: the slow force is a pair sum of the smooth Ewald
+        kernel over all non-excluded pairs, so G with environment-independent
+        coefficients C_b reproduces the part of its change that comes from
+        pairs within rf; the relative loss of those 16 constants, fitted by
+        least squares to the raw change.  Without the field-gradient term
+        they become the output biases (the network's starting point)."""
+        rng = np.random.default_rng(seed)
         self.attach(system)
+        z = init_params(rng)
+        z[W3:SCALE] = 0.0  # G = 0
+        system.learned_set_params(z)
         self._frames(system, self.outer_step, mask)
         f0, v0, s0, _ = system.learned_frame_data(0)
         _, v1, s1, _ = system.learned_frame_data(1)
+        self.baseline_loss = system.learned_train_step(1e-30, 1)
         mu = f0.mean(axis=0)
         sd = f0.std(axis=0)
         sig = np.where(sd > 1e-6, 1.0 / np.maximum(sd, 1e-6), 1.0)
@@ -132,8 +145,9 @@ class LearnedSlowForce:
         c, *_ = np.linalg.lstsq(dv, dt, rcond=None)
         res = dv @ c - dt
         self.pair_model_loss = float(np.sum(res ** 2) / max(np.sum(dt ** 2), 1e-300))
-        self.params = init_params(np.random.default_rng(seed), mu, sig, scale)
-        self.params[B3:SCALE] = (c / scale).astype(np.float32)
+        self.params = init_params(rng, mu, sig, scale)
+        if not self.field_gradient:
+            self.params[B3:SCALE] = (c / scale).astype(np.float32)
         system.learned_set_params(self.params)
 
     def train(self, system, iterations=400, lr=2e-3, temperatures=(280.0, 320.0), dt=1.0,

@@ -83,6 +83,7 @@ def test_train_step_loss_and_gradient_sign(lib):
     s.learned_config(RF, 1.0, 256)
     p = _params(2, scale=0.05)
     s.learned_set_params(p)
+    s.learned_set_terms(False, True)
     s.learned_frame(0)
     s.integrate(3, ens.term_mask, want_energy=False)
     s.learned_frame(1)
@@ -135,6 +136,7 @@ def test_learned_held_force_equations(lib):
 
     s.learned_config(RF, 1.0, 256)
     s.learned_set_params(_params(3, zero_out=True))
+    s.learned_set_terms(False, True)
     s.integrator_config(lib.INTEGRATOR_VERLET, 1.0)
     k = 4
     s.set_mts_learned(k, 1e9)
@@ -187,6 +189,7 @@ def test_judge_falls_back_to_impulse(lib):
 
     s.learned_config(RF, 1.0, 256)
     s.learned_set_params(_params(4, zero_out=True))
+    s.learned_set_terms(False, True)
     s.integrator_config(lib.INTEGRATOR_VERLET, 1.0)
     k = 4
     s.set_mts_learned(k, 1e-12)
@@ -299,3 +302,51 @@ def test_tensor_core_kernel_matches_simt(lib):
         return np.sqrt(np.mean(d ** 2))
 
     assert dist(pos[0], pos[1]) < 1e-2 * dist(pos[0], pos[2])
+
+
+def test_field_gradient_term_vs_finite_differences(lib):
+    """With the field-gradient term alone, an inner step's slow force is
+    F_slow(x0) + J (x1 - x0) with J_i = d F_slow,i / d x_i: compared with J
+    from central differences of the slow force (atom i moved alone)."""
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(900, 30.0, seed=11)
+    ens = _ensemble(w)
+    probe = _ensemble(w)
+    s, mask = ens.system, ens.term_mask
+    recip = lib.mask(lib.TERM_COUL_RECIP)
+    fast = mask & ~recip
+
+    def forces(x, terms):
+        probe.system.set_positions(x)
+        probe.system.compute_forces(terms)
+        return probe.system.get_forces()
+
+    s.learned_config(RF, 1.0, 256)
+    s.learned_set_params(_params(8, zero_out=True))
+    s.learned_set_terms(True, False)
+    s.integrator_config(lib.INTEGRATOR_VERLET, 1.0)
+    s.set_mts_learned(4, 1e9)
+    x0 = w.positions.copy()
+    f_slow0 = forces(x0, recip)
+    s.integrate(1, mask, want_energy=False)
+    x1 = s.get_positions()
+    dx = x1 - x0
+    dx -= w.box * np.round(dx / w.box)
+    pred = s.get_forces() - forces(x1, fast) - f_slow0     # J (x1 - x0)
+    atoms = [3 * m + a for m in (5, 200, 451, 777) for a in range(3)]
+    h = 0.01
+    err, ref = [], []
+    for i in atoms:
+        J = np.zeros((3, 3))
+        for a in range(3):
+            xp, xm = x0.copy(), x0.copy()
+            xp[i, a] += h
+            xm[i, a] -= h
+            J[:, a] = (forces(xp, recip)[i] - forces(xm, recip)[i]) / (2 * h)
+        fd = J @ dx[i]
+        err.append(pred[i] - fd)
+        ref.append(fd)
+    err, ref = np.array(err), np.array(ref)
+    # (B-spline second derivatives of an order-4 PME grid of ~0.94 A spacing)
+    assert np.sqrt(np.mean(err ** 2)) < 0.15 * np.sqrt(np.mean(ref ** 2))
