@@ -12,6 +12,12 @@ step is one CUDA-graph replay bracketed by CUDA events on the launching
 stream; a 256 MB buffer is rewritten between timed steps to flush the 129 MB
 L2 (the working set, ~25 MB, would otherwise stay L2-resident).
 
+Beside the plain form it times the multiple-time-step forms on the same
+system: the impulse scheme with PME every k steps (--mts) and the learned
+slow force with PME every k steps (--learned; trained first on frame pairs
+of a plain Langevin run at 280-320 K).  Each form's NVE drift (100 ps after
+20 ps of Langevin) gates it; "chosen" is the fastest form that passes.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 N > 1 runs one independent replica per GPU (torchrun; the path does not

@@ -525,6 +525,6 @@ cudaError_t ls_after_join(mdg_system *s, int phase);  // main stream: judge, com
 cudaError_t ls_refresh_weights(mdg_system *s);
 cudaError_t ls_train(mdg_system *s, float lr, int t, double *loss);
 cudaError_t ls_predict(mdg_system *s, int slot);
-cudaError_t ls_mlp_tc(mdg_system *s, int slot, int apply);  // mdg_learned_tc.cu
+cudaError_t ls_mlp_tc(mdg_system *s, int slot);  // mdg_learned_tc.cu
 int ls_tc_prepare(mdg_system *s);
 }  // namespace mdg

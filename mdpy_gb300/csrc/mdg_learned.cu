@@ -12,12 +12,14 @@
 // 64 -> 128 -> 128 -> 16 with SiLU and FP32 accumulation, whose 16 outputs
 // are coefficients on the vectors S_ib = q_i sum_j q_j psi_b(r_ij) d_ij / rf^2
 // (16 cubic B-spline radial functions psi_b, d_ij = x_i - x_j):
-//     G_i = sum_b C_ib S_ib.
-// Every k-th step the full PME result judges the prediction (relative RMS
-// error against the total force); above the threshold the next interval
-// falls back to the impulse scheme (the slow force enters at the interval's
-// end with weight k), and the judge keeps running so the learned form
-// resumes once its error is back under the threshold.
+//     G_i = sum_b C_ib S_ib
+// (optionally plus J_i (x_i(t) - x_i(t0)), the atom's motion through the
+// field of the others).  Every k-th step the full PME result judges the
+// prediction (relative RMS error against the total force); above the
+// threshold the next interval falls back to the impulse scheme (the slow
+// force enters at the interval's end with weight k), and the judge keeps
+// running so the learned form resumes once its error is back under the
+// threshold.
 //
 // Kernels (one system; atom order unless stated):
 //   k_ls_pos       FP64 x -> wrapped FP32 positions; motion since the list
@@ -31,6 +33,9 @@
 //                  shared memory
 //   k_ls_mlp       SIMT MLP (training forward, and the reference for the
 //                  tensor-core kernel of mdg_learned_tc.cu)
+//   k_ls_hessian / k_ls_hessian_excl
+//                  optional field-gradient term J_i = d F_slow,i / d x_i
+//   k_ls_apply     inner steps: f += F_slow(t0) - G(t0) + G(t) [+ J dx]
 //   k_ls_judge     relative error of the prediction, mode of the next interval
 //   k_ls_combine   slow force into f with the interval's weight; new base
 //   training: k_ls_target, k_ls_residual, k_ls_dout, k_ls_backward,
@@ -414,13 +419,9 @@ constexpr size_t kMlpSmem =
     sizeof(float) * (2 * kLsHidden + kLsVec);
 
 // One 128-atom tile per CTA of 256 threads; layers 1 and 2 give each thread an
-// 8 x 8 block of the tile's outputs.  TRAIN keeps the pre-activations; APPLY
-// (an inner step in the learned mode) adds base + G to the force words.
-template <bool TRAIN, bool APPLY>
-__global__ void __launch_bounds__(256) k_ls_mlp(Learned L, Geo g, int slot,
-                                                unsigned long long *__restrict__ f,
-                                                const int *__restrict__ inv_perm) {
-    if (APPLY && *L.mode != kLsLearned) return;
+// 8 x 8 block of the tile's outputs.  TRAIN keeps the pre-activations.
+template <bool TRAIN>
+__global__ void __launch_bounds__(256) k_ls_mlp(Learned L, Geo g, int slot) {
     extern __shared__ __align__(16) unsigned char smraw[];
     uint16_t *Xs = (uint16_t *)smraw;
     uint16_t *W1s = Xs + kLsTile * kLsFeat;
@@ -502,12 +503,6 @@ __global__ void __launch_bounds__(256) k_ls_mlp(Learned L, Geo g, int slot,
         for (int d = 0; d < 3; ++d) {
             gv[d] += red[3 * row + d];
             L.G[slot][(size_t)d * g.n_rows + gr] = gv[d];
-        }
-        if (APPLY && gr < g.n) {
-            const int k = inv_perm[gr];
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
-                fix_red(&f[(size_t)d * g.n_pad + k], L.base[(size_t)d * g.n + gr] + to_fix(gv[d]));
         }
     }
 }
@@ -1143,11 +1138,9 @@ int ls_configure(mdg_system *s, float rf, float skin, int cap) {
     if (cudaMemcpy(L->params, p.data(), sizeof(float) * kLsParams, cudaMemcpyHostToDevice) !=
         cudaSuccess)
         return MDG_ERR_CUDA;
-    if (cudaFuncSetAttribute(k_ls_mlp<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_ls_mlp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kMlpSmem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_ls_mlp<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kMlpSmem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_ls_mlp<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_ls_mlp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kMlpSmem) != cudaSuccess ||
         cudaFuncSetAttribute(k_ls_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kBwdSmem) != cudaSuccess)
@@ -1209,7 +1202,7 @@ cudaError_t ls_refresh_weights(mdg_system *s) {
     s->launches += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return ls_mlp_tc(s, -1, 0);  // -1: lay out the tensor-core operand copy
+    return ls_mlp_tc(s, -1);  // -1: lay out the tensor-core operand copy
 }
 
 // Side-stream part of an evaluation (after PME): positions, the neighbour
@@ -1254,12 +1247,12 @@ cudaError_t ls_side(mdg_system *s, int phase) {
         else k_ls_features<false><<<fb, kFeatThreads, 0, st>>>(L, g, slot, gated);
         s->launches += 1;
         if (phase == kLsFrame) {
-            k_ls_mlp<true, false><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, slot, s->f, s->inv_perm);
+            k_ls_mlp<true><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, slot);
             s->launches += 1;
         } else if (L.use_tc) {
-            e = ls_mlp_tc(s, 0, 0);
+            e = ls_mlp_tc(s, 0);
         } else {
-            k_ls_mlp<false, false><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, 0, s->f, s->inv_perm);
+            k_ls_mlp<false><<<L.n_tiles, 256, kMlpSmem, st>>>(L, g, 0);
             s->launches += 1;
         }
         if (e == cudaSuccess) e = cudaGetLastError();
@@ -1296,9 +1289,9 @@ cudaError_t ls_after_join(mdg_system *s, int phase) {
 // kernel the launch setting selects; G[slot] then holds the prediction.
 cudaError_t ls_predict(mdg_system *s, int slot) {
     Learned &L = *s->ls;
-    if (L.use_tc) return ls_mlp_tc(s, slot, 0);
+    if (L.use_tc) return ls_mlp_tc(s, slot);
     const Geo g = make_geo(s);
-    k_ls_mlp<false, false><<<L.n_tiles, 256, kMlpSmem, s->stream>>>(L, g, slot, s->f, s->inv_perm);
+    k_ls_mlp<false><<<L.n_tiles, 256, kMlpSmem, s->stream>>>(L, g, slot);
     s->launches += 1;
     return cudaGetLastError();
 }

@@ -10,8 +10,7 @@
 // to an mbarrier.  Each warp then reads its 32 accumulator lanes (one atom
 // per thread) with tcgen05.ld, adds the bias, applies SiLU, and writes the
 // BF16 activations back to shared memory as the next layer's A operand.
-// The last epilogue forms G_i = sum_b C_ib S_ib and, on inner steps of the
-// learned form, adds base + G to the force words.
+// The last epilogue forms G_i = sum_b C_ib S_ib.
 //
 // Operand layout (shared memory and the prepared global weight copy): no
 // swizzle, K-major, 8 x 16-byte core matrices, K-chunk-major: element
@@ -187,11 +186,8 @@ __device__ __forceinline__ void epilogue_hidden(uint32_t taddr, const float *bia
     }
 }
 
-template <bool APPLY>
 __global__ void __launch_bounds__(kTcThreads, 2)
-    k_ls_mlp_tc(Learned L, int n, int n_rows, int n_pad, int slot, unsigned long long *f,
-                const int *__restrict__ inv_perm, int *status) {
-    if (APPLY && *L.mode != kLsLearned) return;
+    k_ls_mlp_tc(Learned L, int n_rows, int slot, int *status) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const int t = threadIdx.x, w = t >> 5;
     uint16_t *Hs = (uint16_t *)(sm + kOffH);
@@ -317,12 +313,6 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         }
 #pragma unroll
         for (int d = 0; d < 3; ++d) L.G[slot][(size_t)d * n_rows + row] = gv[d];
-        if (APPLY && row < n) {
-            const int k = inv_perm[row];
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
-                fix_red(&f[(size_t)d * n_pad + k], L.base[(size_t)d * n + row] + to_fix(gv[d]));
-        }
         fence_before();  // accumulator reads before the next tile's MMAs
     }
     if (t == 0) {
@@ -365,16 +355,14 @@ __global__ void __launch_bounds__(256) k_ls_tc_layout(Learned L) {
 }  // namespace
 
 int ls_tc_prepare(mdg_system *) {
-    if (cudaFuncSetAttribute(k_ls_mlp_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kTcSmemAlloc) != cudaSuccess ||
-        cudaFuncSetAttribute(k_ls_mlp_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_ls_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              kTcSmemAlloc) != cudaSuccess)
         return MDG_ERR_CUDA;
     return MDG_OK;
 }
 
 // slot < 0: lay out the weight images; else the forward pass of `slot`
-cudaError_t ls_mlp_tc(mdg_system *s, int slot, int apply) {
+cudaError_t ls_mlp_tc(mdg_system *s, int slot) {
     Learned &L = *s->ls;
     cudaStream_t st = s->stream;
     if (slot < 0) {
@@ -383,12 +371,7 @@ cudaError_t ls_mlp_tc(mdg_system *s, int slot, int apply) {
         return cudaGetLastError();
     }
     const int grid = std::min(L.n_tiles, 2 * std::max(1, s->n_sms));
-    if (apply)
-        k_ls_mlp_tc<true><<<grid, kTcThreads, kTcSmemAlloc, st>>>(L, s->n, L.n_rows, s->n_pad, slot,
-                                                                  s->f, s->inv_perm, s->status);
-    else
-        k_ls_mlp_tc<false><<<grid, kTcThreads, kTcSmemAlloc, st>>>(
-            L, s->n, L.n_rows, s->n_pad, slot, s->f, s->inv_perm, s->status);
+    k_ls_mlp_tc<<<grid, kTcThreads, kTcSmemAlloc, st>>>(L, L.n_rows, slot, s->status);
     s->launches += 1;
     return cudaGetLastError();
 }
