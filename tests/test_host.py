@@ -315,3 +315,20 @@ def test_learned_reference_features_brute_force():
     fb, vb = R.features(c @ rot.T + 50.0, q[:30], big, rf)
     assert np.allclose(fa, fb, atol=1e-10)
     assert np.allclose(np.einsum("ab,nkb->nka", rot, va), vb, atol=1e-10)
+
+
+def test_learned_save_load_round_trip(tmp_path):
+    """LearnedSlowForce keeps its parameters and settings through save/load
+    (host logic only)."""
+    from mdpy_gb300 import learned as Lr
+
+    p = Lr.init_params(np.random.default_rng(3), scale=0.5)
+    a = Lr.LearnedSlowForce(outer_step=3, threshold=0.02, rf=5.5, skin=1.2, list_capacity=200,
+                            params=p)
+    path = str(tmp_path / "slow_force.npz")
+    a.save(path)
+    b = Lr.LearnedSlowForce.load(path)
+    assert np.array_equal(a.params, b.params)
+    assert (b.outer_step, b.threshold, b.rf, b.skin, b.list_capacity) == (3, 0.02, 5.5, 1.2, 200)
+    with pytest.raises(ValueError):
+        Lr.LearnedSlowForce(outer_step=1)
