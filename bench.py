@@ -685,10 +685,13 @@ def main():
                        else None)
     e2e_value = unit.ns_per_day(world * a.e2e_steps / e2e_s, DT_FS)
     e2e = {"value": e2e_value, "unit": "ns/day", "h2d_bytes_per_step": 2 * n * 24,
-           "d2h_bytes_per_step": 2 * n * 24 + 8 * (_lib.NUM_TERMS + 1),
-           "api": "mdg_step_host: positions + velocities in from pinned host memory, one "
-                  "step (starting with a re-sort, as new host positions require), wrapped "
-                  "positions + velocities + energies out, one synchronisation"}
+           "d2h_bytes_per_step": 2 * n * 24 + 8 * (_lib.NUM_TERMS + 1) + 4,
+           "api": "mdg_step_host: positions + velocities in from pinned host memory (the "
+                  "previous call's outputs), one step, wrapped positions + velocities + "
+                  "energies out; the incoming positions are compared on the device with the "
+                  "state (one 4-byte read and a synchronisation), and equal ones keep their "
+                  "forces and cluster order -- other positions trigger a re-sort and a fresh "
+                  "force evaluation"}
 
     # what a multiple-time-step scheme could save at most: the same step
     # with the reciprocal-space term left out (PME runs beside the pair
@@ -753,12 +756,30 @@ def main():
         forms.append(f)
         learned_forms[id(f)] = lrn
 
-    nve = nve_drift(sysm, mask, n, a.nve_ps) if a.nve_ps > 0 else None
+    # every NVE run starts from the same state, and the state is put back
+    # afterwards (a form whose run diverges must not spoil what follows)
+    x_keep, v_keep = sysm.get_positions(), sysm.get_velocities()
+
+    def restore():
+        sysm.set_mts(1)
+        sysm.set_positions(x_keep)
+        sysm.set_velocities(v_keep)
+        sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 4243)
+
+    def drift_of(**kw):
+        try:
+            return nve_drift(sysm, mask, n, a.nve_ps, **kw)
+        except Exception as e:  # noqa: BLE001 -- a diverging form is a result
+            return {"diverged": "%s: %s" % (type(e).__name__, e),
+                    "kT_per_ns_per_atom": None, "stderr_kT_per_ns_per_atom": None}
+        finally:
+            restore()
+
+    nve = drift_of() if a.nve_ps > 0 else None
     if a.nve_ps > 0:
         for f in forms:
-            f["nve_drift"] = nve_drift(sysm, mask, n, a.nve_ps, mts=f.get("mts", 1), seed=1,
-                                       learned=learned_forms.get(id(f)))
-        sysm.set_mts(1)
+            f["nve_drift"] = drift_of(mts=f.get("mts", 1), seed=1,
+                                      learned=learned_forms.get(id(f)))
 
     err = None
     cpu = None
@@ -778,7 +799,11 @@ def main():
         # shown to exceed 1e-3 kT/ns/atom (|drift| - 2 standard errors)
         def within(f):
             d = f.get("nve_drift")
-            return d is None or abs(d["kT_per_ns_per_atom"]) - 2 * d["stderr_kT_per_ns_per_atom"] <= 1e-3
+            if d is None:
+                return True
+            if d.get("kT_per_ns_per_atom") is None:  # the run diverged
+                return False
+            return abs(d["kT_per_ns_per_atom"]) - 2 * d["stderr_kT_per_ns_per_atom"] <= 1e-3
         chosen = max([plain] + [f for f in forms if within(f)], key=lambda f: f["ns_per_day"])
         line = {
             "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world,

@@ -175,8 +175,12 @@ MDG_API int mdg_kinetic_energy(mdg_system *sys, double *kinetic);
  * the configured integrator on the terms in `mask`, copies the wrapped
  * positions, the velocities (host (n,3); NULL = skip) and the energies
  * (energies[MDG_NUM_TERMS], *kinetic; NULL = skip) back, all on the system's
- * stream with one synchronisation at the end.  New positions start with a
- * re-sort, as mdg_set_positions does. */
+ * stream with one synchronisation at the end.  Incoming positions are
+ * compared on the device with the state as it would be reported (one more
+ * synchronisation): equal ones -- the previous call's outputs fed back --
+ * keep the forces already computed for them and the cluster order; others
+ * start with a re-sort and a fresh force evaluation, as mdg_set_positions
+ * does. */
 MDG_API int mdg_step_host(mdg_system *sys, const double *x_in, const double *v_in, int n_steps,
                           unsigned mask, double *x_out, double *v_out, double *energies,
                           double *kinetic);

@@ -553,6 +553,8 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     if (s->host_stage) cudaFreeHost(s->host_stage);
+    dfree(s->xin);
+    dfree(s->same_flag);
     delete s;
     return MDG_OK;
 }
@@ -1305,18 +1307,41 @@ MDG_API int mdg_step_host(mdg_system *s, const double *x_in, const double *v_in,
                           double *kinetic) {
     int rc = check_sys(s);
     if (rc) return rc;
+    const size_t ne = (size_t)kEnergySlots * s->n_sys;
     if (!s->host_stage) {
-        // pinned staging for the energy words and the status word
-        const size_t bytes = sizeof(long long) * (kEnergySlots * (size_t)s->n_sys + 1);
-        CK(cudaMallocHost((void **)&s->host_stage, bytes), "pinned staging");
+        // pinned staging for the energy words, the status word and the
+        // positions-comparison flag
+        CK(cudaMallocHost((void **)&s->host_stage, sizeof(long long) * (ne + 2)),
+           "pinned staging");
+        int rc2 = dalloc(&s->xin, 3 * (size_t)s->n);
+        if (!rc2) rc2 = dalloc(&s->same_flag, 1);
+        if (rc2) return fail(rc2, "step_host staging");
     }
     if (x_in) {
-        CK(cudaMemcpyAsync(s->x, x_in, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice,
+        // Positions that equal the state (as the previous call returned it)
+        // keep the forces already computed for them, and the cluster order:
+        // the copy lands beside the state and one comparison decides.
+        bool same = false;
+        CK(cudaMemcpyAsync(s->xin, x_in, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice,
                            s->stream),
            "copy positions");
-        s->have_x = 1;
-        s->need_reorder = 1;
-        s->forces_valid = 0;
+        if (s->have_x && s->forces_valid) {
+            CK(cudaMemsetAsync(s->same_flag, 0, sizeof(int), s->stream), "memset");
+            CK(launch_same_positions(s, s->xin, s->same_flag), "compare positions");
+            CK(cudaMemcpyAsync(s->host_stage + ne + 1, s->same_flag, sizeof(int),
+                               cudaMemcpyDeviceToHost, s->stream),
+               "flag read");
+            CK(cudaStreamSynchronize(s->stream), "synchronize");
+            same = ((int)(s->host_stage[ne + 1] & 0xffffffffll)) == 0;
+        }
+        if (!same) {
+            CK(cudaMemcpyAsync(s->x, s->xin, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
+                               s->stream),
+               "copy positions");
+            s->have_x = 1;
+            s->need_reorder = 1;
+            s->forces_valid = 0;
+        }
     }
     if (v_in) {
         CK(cudaMemcpyAsync(s->v, v_in, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice,
@@ -1341,7 +1366,6 @@ MDG_API int mdg_step_host(mdg_system *s, const double *x_in, const double *v_in,
                            s->stream),
            "copy velocities");
     long long *stage = s->host_stage;
-    const size_t ne = (size_t)kEnergySlots * s->n_sys;
     if (want_energy)
         CK(cudaMemcpyAsync(stage, s->energy, sizeof(long long) * ne, cudaMemcpyDeviceToHost,
                            s->stream),

@@ -263,6 +263,31 @@ cudaError_t launch_forces_out(mdg_system *s) {
     return cudaGetLastError();
 }
 
+// flag |= 1 unless xin equals, bit for bit, what k_positions_out reports for x
+__global__ void k_same_positions(const double *__restrict__ x, int n,
+                                 const SysDev *__restrict__ sys, const int *__restrict__ atom_sys,
+                                 const double *__restrict__ xin, int *flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool differ = false;
+    if (i < n) {
+        const double *L = sys[atom_sys[i]].Ld;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double p = x[3 * i + d];
+            const double inv32 = (double)(float)(1.0 / L[d]);
+            differ |= xin[3 * i + d] != p - L[d] * rint(p * inv32);
+        }
+    }
+    if (__any_sync(0xffffffffu, differ) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+cudaError_t launch_same_positions(mdg_system *s, const double *xin, int *flag) {
+    k_same_positions<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->x, s->n, s->sys_dev,
+                                                                 s->atom_sys, xin, flag);
+    s->launches += 1;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_positions_out(mdg_system *s, double *out) {
     k_positions_out<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->x, s->n, s->sys_dev,
                                                                 s->atom_sys, out);

@@ -423,6 +423,8 @@ struct mdg_system {
     unsigned long long *step_dev = nullptr;
     double *fout = nullptr;            // (n,3) FP64 staging for get_forces
     long long *host_stage = nullptr;   // pinned host staging of mdg_step_host
+    double *xin = nullptr;             // mdg_step_host: incoming positions (3n)
+    int *same_flag = nullptr;          // and their comparison with the state
 
     // launch shapes (set by hand or by mdg_autotune): work items per
     // i-cluster, persistent work-queue form, PME spread/gather block size
@@ -509,6 +511,7 @@ cudaError_t launch_integrate_post(mdg_system *s, int energy);
 cudaError_t launch_kinetic(mdg_system *s);
 cudaError_t launch_forces_out(mdg_system *s);
 cudaError_t launch_positions_out(mdg_system *s, double *out);
+cudaError_t launch_same_positions(mdg_system *s, const double *xin, int *flag);
 cudaError_t launch_noise(mdg_system *s, uint64_t step, float *out);
 cudaError_t launch_sd_step(mdg_system *s, double alpha);
 int prepare_sort_grid(mdg_system *s);   // host: column grid + cluster-order buffers

@@ -199,6 +199,44 @@ def test_step_host_equals_separate_calls(lib):
     assert np.array_equal(a.get_positions(), xb) and a.get_energies()[1] == keb2
 
 
+def test_step_host_continuation_keeps_forces(lib):
+    """Feeding mdg_step_host the positions and velocities it returned
+    continues the trajectory bit for bit as mdg_integrate does (the forces of
+    those positions are kept, no re-sort); changed positions start afresh,
+    as mdg_set_positions does."""
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(600, 26.0, seed=13)
+    ea_, eb_ = _ensemble(w, rc=10.0, K=27), _ensemble(w, rc=10.0, K=27)
+    a, b = ea_.system, eb_.system
+    mask = ea_.term_mask
+    for s in (a, b):
+        s.integrator_config(lib.INTEGRATOR_LANGEVIN, 1.0, 300.0, 0.001, 5)
+    x = np.ascontiguousarray(w.positions)
+    v = np.ascontiguousarray(w.velocities)
+    a.set_positions(x)
+    a.set_velocities(v)
+    xb, vb = x.copy(), v.copy()
+    eb = np.zeros(lib.NUM_TERMS)
+    for step in range(25):   # crosses the re-sort after 20 steps
+        a.integrate(1, mask, want_energy=True)
+        keb = b.step_host_ptr(xb.ctypes.data, vb.ctypes.data, 1, mask, xb.ctypes.data,
+                              vb.ctypes.data, eb)
+        assert np.array_equal(a.get_positions(), xb), step
+        assert np.array_equal(a.get_velocities(), vb), step
+        ea, kea = a.get_energies()
+        assert np.array_equal(ea, eb) and kea == keb, step
+    # moved positions: the forces are recomputed, as after mdg_set_positions
+    xm = np.ascontiguousarray(xb + 1e-3)
+    vm = vb.copy()
+    a.set_positions(xm)
+    a.set_velocities(vm)
+    a.integrate(1, mask, want_energy=True)
+    a.check_status()
+    b.step_host_ptr(xm.ctypes.data, vm.ctypes.data, 1, mask, xb.ctypes.data, vb.ctypes.data, eb)
+    assert np.array_equal(a.get_positions(), xb) and np.array_equal(a.get_velocities(), vb)
+
+
 def test_mts_impulse_equations(lib):
     """Multiple time steps, k = 2: the steps follow the impulse (Verlet-I)
     equations restated in numpy from the library's own term forces -- the
