@@ -266,13 +266,16 @@ __global__ void __launch_bounds__(256) k_convolve(float2 *__restrict__ gc,
     if (i < total) {
         const float2 c = gc[i];
         const float g = G[i];
+        // G = 0 (k = 0 and the padding between members): the element is
+        // dropped whatever it holds
+        const bool live = g != 0.f;
         if (ENERGY) {
             const int kz = (int)((i % nc) % Kh);
             const float wgt = (kz == 0 || (2 * kz == K2)) ? 1.0f : 2.0f;
-            e = (double)(0.5f * wgt * g * (c.x * c.x + c.y * c.y));
+            e = live ? (double)(0.5f * wgt * g * (c.x * c.x + c.y * c.y)) : 0.0;
             q = sys_ids[i / nc];
         }
-        gc[i] = make_float2(c.x * g, c.y * g);
+        gc[i] = live ? make_float2(c.x * g, c.y * g) : make_float2(0.f, 0.f);
     }
     if (ENERGY) {
         const double v[1] = {e};
@@ -493,7 +496,13 @@ int pme_setup(mdg_system *s, const int *grids) {
     if (cudaMalloc(&p.grid_r, roff * sizeof(float)) != cudaSuccess) return MDG_ERR_NOMEM;
     if (cudaMalloc(&p.grid_c, coff * sizeof(float2)) != cudaSuccess) return MDG_ERR_NOMEM;
     if (cudaMalloc(&p.influence, coff * sizeof(float)) != cudaSuccess) return MDG_ERR_NOMEM;
-    if (cudaMemset(p.grid_i, 0, roff * sizeof(long long)) != cudaSuccess) return MDG_ERR_CUDA;
+    // the padding between members' grids is never written by cuFFT: zero it
+    // once (and the convolution keeps it zero), so no stale bits of a freed
+    // buffer reach the energy sum
+    if (cudaMemset(p.grid_i, 0, roff * sizeof(long long)) != cudaSuccess ||
+        cudaMemset(p.grid_r, 0, roff * sizeof(float)) != cudaSuccess ||
+        cudaMemset(p.grid_c, 0, coff * sizeof(float2)) != cudaSuccess)
+        return MDG_ERR_CUDA;
     const double pi = 3.14159265358979323846;
     const double b2 = p.beta * p.beta;
     std::vector<float> G(coff);
