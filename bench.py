@@ -61,7 +61,7 @@ def parse():
                         "waters (1M atoms) in a 215 A box; batch256: 256 independent water "
                         "boxes of 1.5k-12k atoms in one batch")
     p.add_argument("--boxes", type=int, default=256)
-    p.add_argument("--mts", default="2,4",
+    p.add_argument("--mts", default="2,3,4",
                    help="outer steps (in steps) of the multiple-time-step forms timed beside the "
                         "plain one, comma separated (empty: none)")
     p.add_argument("--learned", default="4",
