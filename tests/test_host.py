@@ -332,3 +332,67 @@ def test_learned_save_load_round_trip(tmp_path):
     assert (b.outer_step, b.threshold, b.rf, b.skin, b.list_capacity) == (3, 0.02, 5.5, 1.2, 200)
     with pytest.raises(ValueError):
         Lr.LearnedSlowForce(outer_step=1)
+
+
+class _FakeLearnedSystem:
+    """Records the calls LearnedSlowForce makes (host logic only)."""
+
+    def __init__(self, n=10):
+        self.n = n
+        self.calls = []
+        self.rng = np.random.default_rng(0)
+        self.params = None
+
+    def __getattr__(self, name):
+        def rec(*args, **kw):
+            self.calls.append((name, args))
+        return rec
+
+    def learned_set_params(self, p):
+        self.calls.append(("learned_set_params", ()))
+        self.params = np.array(p, dtype=np.float32)
+
+    def learned_params(self):
+        return self.params.copy()
+
+    def learned_frame_data(self, slot):
+        n = self.n
+        return (self.rng.normal(size=(n, 64)).astype(np.float32),
+                self.rng.normal(size=(n, 16, 3)).astype(np.float32),
+                self.rng.normal(size=(n, 3)).astype(np.float32),
+                np.zeros((n, 3), np.float32))
+
+    def learned_train_step(self, lr, t):
+        self.calls.append(("learned_train_step", (lr, t)))
+        return 1.0 / t
+
+
+def test_learned_training_loop_host_logic():
+    """LearnedSlowForce.train: frame pairs 1..k steps apart after
+    `decorrelate` steps, one Adam step each with a cosine-decayed rate, the
+    Langevin temperature redrawn in the given range, the plain form on."""
+    from mdpy_gb300 import _lib, learned as Lr
+
+    s = _FakeLearnedSystem()
+    lrn = Lr.LearnedSlowForce(outer_step=3)
+    losses = lrn.train(s, iterations=7, lr=1e-2, temperatures=(280.0, 320.0), decorrelate=5,
+                       redraw_every=3, mask=_lib.MASK_ALL, seed=1)
+    assert len(losses) == 7 and lrn.params is not None
+    names = [c[0] for c in s.calls]
+    assert ("set_mts_learned", (0, 1.0)) in s.calls          # plain method makes the frames
+    # normalise: G = 0 parameters, one frame pair k steps apart, a zero-rate step
+    steps = [c for c in s.calls if c[0] == "learned_train_step"]
+    assert steps[0][1] == (1e-30, 1)
+    train = steps[1:]
+    assert [t for _, (_, t) in train] == list(range(1, 8))
+    rates = [r for _, (r, _) in train]
+    assert rates[0] == pytest.approx(1e-2) and all(a > b for a, b in zip(rates, rates[1:]))
+    assert rates[-1] > 1e-3
+    # per iteration: integrate(decorrelate), frame 0, integrate(gap), frame 1
+    ints = [c[1][0] for c in s.calls if c[0] == "integrate"]
+    gaps = ints[1:][1::2]     # after normalise's pair: decorrelate, gap, decorrelate, gap ...
+    assert ints[0] == 3 and gaps == [1, 2, 3, 1, 2, 3, 1]
+    assert all(d == 5 for d in ints[1:][0::2])
+    temps = [c[1][2] for c in s.calls if c[0] == "integrator_config" and c[1][0] == _lib.INTEGRATOR_LANGEVIN]
+    assert len(temps) >= 1 + 3 and all(280.0 <= t <= 320.0 for t in temps)
+    assert names.count("learned_frame") == 2 * 8
