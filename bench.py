@@ -72,6 +72,10 @@ def parse():
     p.add_argument("--learned-threshold", type=float, default=0.05,
                    help="judge threshold of the learned forms (RMS slow-force error over RMS "
                         "total force) above which an interval falls back to the impulse scheme")
+    p.add_argument("--profile-learned", type=int, default=0, metavar="K",
+                   help="profiling run of the learned form only: the water90k box, feature "
+                        "normalisation from one frame pair (no training), 40 plain steps, "
+                        "then 40 learned steps with PME every K steps; prints the times")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch shape instead of timing the alternatives")
     p.add_argument("--waters", type=int, default=None)
@@ -529,8 +533,39 @@ def run_reference_arm(a, world, rank):
     return 0
 
 
+def profile_learned(a):
+    """The short run the learned form's profiles are captured on."""
+    import torch
+
+    from mdpy_gb300 import _lib
+    from mdpy_gb300.learned import LearnedSlowForce
+
+    s = make_system(a, 0)
+    ens, _ = make_ensemble(s, 0, a.grid)
+    sysm, mask = ens.system, ens.term_mask
+    sysm.set_graph_mode(_lib.GRAPH_STEP)
+    lrn = LearnedSlowForce(outer_step=a.profile_learned, threshold=1e9)
+    sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 5)
+    lrn.normalise(sysm, mask)
+    out = {}
+    for name in ("plain", "learned"):
+        if name == "learned":
+            lrn.enable(sysm)
+        sysm.integrate(12, mask, want_energy=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sysm.integrate(40, mask, want_energy=False)
+        torch.cuda.synchronize()
+        out[name + "_ms_per_step"] = (time.perf_counter() - t0) / 40 * 1e3
+    out["judge"] = sysm.learned_stats()
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     a = parse()
+    if a.profile_learned:
+        return profile_learned(a)
     world, rank, local = dist_setup()
     if a.impl == "reference":
         return run_reference_arm(a, world, rank)
