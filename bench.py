@@ -15,8 +15,12 @@ L2 (the working set, ~25 MB, would otherwise stay L2-resident).
 Beside the plain form it times the multiple-time-step forms on the same
 system: the impulse scheme with PME every k steps (--mts) and the learned
 slow force with PME every k steps (--learned; trained first on frame pairs
-of a plain Langevin run at 280-320 K).  Each form's NVE drift (100 ps after
-20 ps of Langevin) gates it; "chosen" is the fastest form that passes.
+of a plain Langevin run at 280-320 K).  Every form, plain included, is gated
+twice: the force the integrator applies on each step of one outer cycle
+must lie within 1e-4 relative RMS of the FP64 force at the same positions
+(largest over the cycle), and its NVE energy drift over 100 ps (after one
+shared Langevin equilibration) must satisfy |drift| + 2 sigma <= 1e-3
+kT/ns/atom.  "chosen" is the fastest form that passes both.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -42,6 +46,12 @@ DT_FS = 1.0
 TEMPERATURE = 300.0
 FRICTION = 0.001          # 1/ps in 1/fs
 CUTOFF, SWITCH, ORDER, EWALD_TOL = 12.0, 10.0, 4, 1e-5
+FORCE_BAR = 1e-4          # relative RMS force error against FP64
+DRIFT_BAR = 1e-3          # kT / ns / atom
+# the FP64 reference's reciprocal term: PME on a 0.5 A grid at order 8, within
+# ~2e-9 relative of the direct Ewald k-sum (tests/test_oracle_math.py) and
+# ~50x faster than it on the 88k-atom box
+REF_PME_SPACING, REF_PME_ORDER = 0.5, 8
 # single-system workloads: waters, box edge (A), chain beads, PME grid
 WORKLOADS = {"water90k": (30000, 96.5, 500, 96), "water1m": (333333, 215.0, 0, 224)}
 L2_FLUSH_BYTES = 256 << 20
@@ -61,7 +71,7 @@ def parse():
                         "waters (1M atoms) in a 215 A box; batch256: 256 independent water "
                         "boxes of 1.5k-12k atoms in one batch")
     p.add_argument("--boxes", type=int, default=256)
-    p.add_argument("--mts", default="2,3,4",
+    p.add_argument("--mts", default="2,3",
                    help="outer steps (in steps) of the multiple-time-step forms timed beside the "
                         "plain one, comma separated (empty: none)")
     p.add_argument("--learned", default="4",
@@ -83,7 +93,13 @@ def parse():
     p.add_argument("--beads", type=int, default=None)
     p.add_argument("--e2e-steps", type=int, default=100)
     p.add_argument("--kernel-reps", type=int, default=200)
-    p.add_argument("--cpu-seconds", type=float, default=20.0)
+    p.add_argument("--cpu-seconds", type=float, default=20.0,
+                   help="host time of the CPU baseline sample of the GPU arm")
+    p.add_argument("--reference-seconds", type=float, default=75.0,
+                   help="host time the reference arm's --steps + --warmup sampled steps take "
+                        "together")
+    p.add_argument("--equilibrate-ps", type=float, default=40.0,
+                   help="Langevin equilibration before the NVE runs (once, shared by all forms)")
     p.add_argument("--no-error-check", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--nve-ps", type=float, default=None,
@@ -98,9 +114,9 @@ def parse():
     if a.nve_ps is None:
         a.nve_ps = 100.0 if a.workload == "water90k" else 0.0
     if a.workload == "water1m":
-        # the FP64 references (all-pairs Coulomb, direct Ewald k-sum) do not
-        # finish at 1M atoms; the 88k-atom box carries both numbers
-        a.no_error_check = True
+        # the all-pairs Coulomb of the reference's CPU path is 5e11 pair terms
+        # per evaluation at 1M atoms; the 88k-atom box carries that number
+        # (the FP64 force error is still measured, on sampled atoms)
         a.no_cpu_baseline = True
     return a
 
@@ -150,13 +166,15 @@ def make_batch_members(n_boxes, seed):
     for w in ws:
         grid = min(48, max(24, systems.fft_friendly(int(round(w.box[0])))))
         ens = batch.member(w.topology, w.pbc_matrix)
+        nb = C.NonbondedConstraint(w.parameters["nonbonded"], BATCH_CUTOFF, ewald_error=EWALD_TOL)
         ens.add_constraints(
-            C.NonbondedConstraint(w.parameters["nonbonded"], BATCH_CUTOFF, ewald_error=EWALD_TOL),
+            nb,
             C.PMEConstraint(grid_size=grid, ewald_error=EWALD_TOL, real_space_cutoff=BATCH_CUTOFF),
             C.CharmmBondConstraint(w.parameters["bond"]),
             C.CharmmAngleConstraint(w.parameters["angle"]))
         ens.state.set_positions(w.positions)
         ens.state.set_velocities(w.velocities)
+        w.ewald_beta = nb.ewald_beta
         members.append((w, ens, grid))
     return members
 
@@ -218,8 +236,41 @@ def run_batch(a, world, rank, local):
     atom_steps = world * n * a.steps / (ms_total / 1000.0)
     # per-box ns/day averaged over boxes = steps/s of the batch
     ns_day_per_box = unit.ns_per_day(a.steps / (ms_total / 1000.0), DT_FS)
+
+    # the persistent work-queue form of the pair kernel (resident warps pull
+    # (cluster, part) items from a device counter), timed beside the shape
+    # the autotuner chose, same protocol
+    persistent = {}
+    base_shape = {k: shape[k] for k in sysm.SHAPE_FIELDS}
+    for per in (20, 24):
+        sh = dict(base_shape)
+        sh["persistent"] = per
+        sysm.set_launch_shape(**sh)
+        sysm.integrate(3, mask, want_energy=False)
+        reps = max(10, a.steps // 2)
+        persistent["persistent_%d_ctas_per_sm" % per] = {
+            "ms_per_step": time_steps(sysm, mask, reps, stream, flush) / reps, "steps": reps}
+    sysm.set_launch_shape(**base_shape)
+    sysm.integrate(3, mask, want_energy=False)
+    persistent["chosen_shape_ms_per_step"] = ms_step
+
     b.update()
     pe = b.potential_energies
+    # force error against FP64 on four members (smallest, largest, two between),
+    # sampled atoms; the batch's plain force
+    errs = []
+    if rank == 0 and not a.no_error_check:
+        sizes = np.array([m[0].num_particles for m in members])
+        order = np.argsort(sizes)
+        for q in sorted({int(order[0]), int(order[len(order) // 3]),
+                         int(order[2 * len(order) // 3]), int(order[-1])}):
+            w = members[q][0]
+            sub = sample_atoms(w.num_particles, 500, seed=q)
+            ref = reference_forces(w, b.positions(q), w.ewald_beta, sub, cutoff=BATCH_CUTOFF,
+                                   switch=None)
+            errs.append({"member": q, "atoms": int(w.num_particles),
+                         "force_rel_rms_err_vs_fp64": rel_err(b.forces(q)[sub], ref),
+                         "sample_atoms": int(len(sub))})
 
     # the same boxes one at a time: every 8th box, each its own system
     sample = members[::8]
@@ -266,6 +317,10 @@ def run_batch(a, world, rank, local):
                               "sample": "every 8th box (%d boxes, %d atoms) timed alone, scaled "
                                         "by atoms" % (len(sample), single_atoms)},
             "speedup_vs_one_at_a_time": one_at_a_time_ms / ms_step,
+            "persistent_form": persistent,
+            "force_error_members": errs,
+            "force_rel_rms_err_vs_fp64": max(e["force_rel_rms_err_vs_fp64"] for e in errs)
+            if errs else None,
             "finite_energies": bool(np.all(np.isfinite(pe))),
             "gpu_launches": int(launches), "clocks": clk,
         }
@@ -368,165 +423,333 @@ def barrier(world):
         dist.barrier()
 
 
-def nve_drift(sysm, mask, n_atoms, ps, chunk=500, equilibrate_ps=20.0, seed=0, mts=1,
-              learned=None):
-    """Total-energy drift of a velocity-Verlet run of ``ps`` picoseconds:
-    ``equilibrate_ps`` of Langevin at 300 K first (the lattice start relaxes
-    for several ps, which shows as a spurious trend), then the least-squares
-    slope of E(t), sampled every ``chunk`` steps, in kT per ns per atom."""
-    from mdpy_gb300 import _lib, unit
+def integrated_autocorrelation_time(x):
+    """Integrated autocorrelation time of the series x, in samples (0.5 for
+    uncorrelated samples), by Sokal's automatic window (stop at m >= 5 tau)."""
+    x = np.asarray(x, dtype=np.float64) - np.mean(x)
+    n = len(x)
+    if n < 4 or not np.any(x):
+        return 0.5
+    f = np.fft.rfft(x, 2 * n)
+    acf = np.fft.irfft(f * np.conj(f))[:n]
+    acf /= acf[0]
+    tau = 0.5
+    for m in range(1, n):
+        tau += acf[m]
+        if m >= 5.0 * tau:
+            break
+    return max(tau, 0.5)
+
+
+def drift_statistics(t_fs, e_tot, n_atoms, nb=10):
+    """Least-squares slope of E(t) in kT per ns per atom, with the standard
+    error of that slope from the residuals: the residuals' variance over the
+    effective number of independent samples N / (2 tau), tau their
+    integrated autocorrelation time (white noise: tau = 1/2; slow, random-
+    walk-like wander: large tau and a large error).  Also the slopes of nb
+    consecutive blocks."""
+    from mdpy_gb300 import unit
+
+    t = np.asarray(t_fs, dtype=np.float64)
+    e = np.asarray(e_tot, dtype=np.float64)
+    to_kt = 1e6 / (n_atoms * unit.KB * TEMPERATURE)     # energy/fs -> kT/ns/atom
+    coef = np.polyfit(t, e, 1)
+    resid = e - np.polyval(coef, t)
+    tau = integrated_autocorrelation_time(resid)
+    n_eff = max(len(t) / (2.0 * tau), 3.0)
+    span = t[-1] - t[0]
+    sigma = float(np.std(resid, ddof=2) * math.sqrt(12.0 / n_eff) / span) * to_kt
+    lb = len(t) // nb
+    blocks = [float(np.polyfit(t[i * lb:(i + 1) * lb], e[i * lb:(i + 1) * lb], 1)[0]) * to_kt
+              for i in range(nb)] if lb >= 3 else []
+    return {"kT_per_ns_per_atom": float(coef[0]) * to_kt, "stderr_kT_per_ns_per_atom": sigma,
+            "autocorrelation_samples": tau, "effective_samples": n_eff,
+            "block_slopes_kT_per_ns_per_atom": blocks,
+            "energy_rms_fluctuation_kT_per_atom":
+                float(np.std(resid)) * 1.0 / (n_atoms * unit.KB * TEMPERATURE)}
+
+
+def equilibrate(sysm, mask, ps, seed=77):
+    """Langevin at 300 K (the lattice start relaxes for tens of ps)."""
+    from mdpy_gb300 import _lib
 
     sysm.set_mts(1)
-    sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 77 + seed)
-    sysm.integrate(int(equilibrate_ps * 1000.0 / DT_FS), mask, want_energy=False)
+    sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, seed)
+    sysm.integrate(int(ps * 1000.0 / DT_FS), mask, want_energy=False)
+
+
+def nve_drift(sysm, mask, n_atoms, ps, every=20, mts=1, learned=None):
+    """Total-energy drift of a velocity-Verlet run of ``ps`` picoseconds from
+    the current state, sampled every ``every`` steps (rounded up to whole
+    outer steps of a multiple-time-step form); see drift_statistics."""
+    from mdpy_gb300 import _lib
+
     sysm.integrator_config(_lib.INTEGRATOR_VERLET, DT_FS)
+    k = learned.outer_step if learned is not None else mts
+    every = k * int(math.ceil(every / float(k)))
     if learned is not None:
         learned.enable(sysm)
         sysm.learned_reset_stats()
     else:
         sysm.set_mts(mts)
-    n_chunks = max(2, int(round(ps * 1000.0 / DT_FS / chunk)))
+    n_samples = max(8, int(round(ps * 1000.0 / DT_FS / every)))
     terms = [t for t in range(_lib.NUM_TERMS) if mask >> t & 1]
     t_fs, e_tot = [], []
     t0 = time.perf_counter()
-    for k in range(n_chunks):
-        sysm.integrate(chunk, mask, want_energy=True)
+    for i in range(n_samples):
+        sysm.integrate(every, mask, want_energy=True)
         e, ke = sysm.get_energies()
-        t_fs.append((k + 1) * chunk * DT_FS)
+        t_fs.append((i + 1) * every * DT_FS)
         e_tot.append(float(sum(e[t] for t in terms) + ke))
     wall = time.perf_counter() - t0
     judge = sysm.learned_stats() if learned is not None else None
     sysm.set_mts(1)
-    slope = float(np.polyfit(np.array(t_fs), np.array(e_tot), 1)[0])   # energy unit / fs
-    kT = unit.KB * TEMPERATURE
-    drift = slope * 1e6 / (n_atoms * kT)
-    e0 = e_tot[0]
-    half = n_chunks // 2
-    halves = [float(np.polyfit(np.array(t_fs[i:j]), np.array(e_tot[i:j]), 1)[0]) * 1e6
-              / (n_atoms * kT) for i, j in ((0, half), (half, n_chunks))]
-    # standard error of the whole-run slope from the spread of 4 block slopes
-    # (a slope's noise grows as T^-1.5 for a window of length T)
-    nb = 4
-    lb = n_chunks // nb
-    blocks = [float(np.polyfit(np.array(t_fs[i * lb:(i + 1) * lb]),
-                               np.array(e_tot[i * lb:(i + 1) * lb]), 1)[0]) * 1e6
-              / (n_atoms * kT) for i in range(nb)]
-    stderr = float(np.std(blocks, ddof=1)) / nb ** 1.5
-    return {"kT_per_ns_per_atom": drift, "halves_kT_per_ns_per_atom": halves,
-            "block_slopes_kT_per_ns_per_atom": blocks, "stderr_kT_per_ns_per_atom": stderr,
-            "ps": n_chunks * chunk * DT_FS / 1000.0,
-            "samples": n_chunks, "sample_every_steps": chunk,
-            "max_abs_dev_kT_per_atom": float(np.max(np.abs(np.array(e_tot) - e0)) / (n_atoms * kT)),
-            "integrator": "velocity Verlet, dt 1 fs%s, after %g ps of Langevin at 300 K"
-                          % ((", learned slow force, PME every %d steps" % learned.outer_step)
-                             if learned is not None else
-                             (", reciprocal force every %d steps (impulse)" % mts) if mts > 1
-                             else "", equilibrate_ps),
-            "judge": judge, "wall_s": wall}
+    out = drift_statistics(t_fs, e_tot, n_atoms)
+    out.update({
+        "ps": n_samples * every * DT_FS / 1000.0, "samples": n_samples,
+        "sample_every_steps": every,
+        "integrator": "velocity Verlet, dt 1 fs%s" % (
+            (", learned slow force, PME every %d steps" % learned.outer_step)
+            if learned is not None else
+            (", reciprocal force every %d steps (impulse)" % mts) if mts > 1 else ""),
+        "judge": judge, "wall_s": wall})
+    return out
+
+
+def drift_passes(d):
+    """|drift| + 2 standard errors <= the bar: the run must show the drift
+    below the bar, not merely fail to show it above."""
+    if d is None or d.get("kT_per_ns_per_atom") is None:
+        return False
+    return abs(d["kT_per_ns_per_atom"]) + 2.0 * d["stderr_kT_per_ns_per_atom"] <= DRIFT_BAR
+
+
+# --------------------------------------------------------------------------
+# force error vs the FP64 oracle (sampled atoms)
+# --------------------------------------------------------------------------
+def _bonded_rows(s):
+    t = s.topology
+    types = t.particle_types
+    kb = np.array([s.parameters["bond"]["%s-%s" % (types[i], types[j])] for i, j in t.bonds])
+    ka = np.array([s.parameters["angle"]["%s-%s-%s" % (types[i], types[j], types[k])]
+                   for i, j, k in t.angles])
+    return kb, ka
+
+
+def ref_pme_grid(box):
+    from mdpy_gb300 import systems
+
+    return [systems.fft_friendly(int(math.ceil(L / REF_PME_SPACING)), hi=2048)
+            for L in np.broadcast_to(np.asarray(box, float), (3,))]
+
+
+def reference_forces(s, pos, beta, sub, cutoff=CUTOFF, switch=SWITCH):
+    """The FP64 total force on the atoms ``sub`` at positions ``pos``: LJ (+
+    switch) and Ewald real space (cell list), reciprocal space (FP64 PME at
+    0.5 A / order 8), the excluded-pair correction and the bonded terms."""
+    from oracle import oracle as O
+
+    t = s.topology
+    p = s.parameters["nonbonded"]
+    lj = np.array([[p[ty][0], p[ty][1], p[ty][0], p[ty][1]] for ty in t.particle_types])
+    q = t.charges.reshape(-1)
+    f_nb, _ = O.nonbonded(pos, s.box, lj, q, t.bonded_particles, t.scaling_particles, cutoff,
+                          switch=switch, coulomb="ewald", beta=beta, rows=sub)
+    f_rec, _ = O.pme(pos, s.box, q, beta, ref_pme_grid(s.box), REF_PME_ORDER)
+    f_ex, _ = O.ewald_exclusions(pos, s.box, q, t.bonded_particles, beta)
+    kb, ka = _bonded_rows(s)
+    f_b, _ = O.bonds(pos, s.box, t.bonds, kb)
+    f_a, _ = O.angles(pos, s.box, t.angles, ka)
+    f_d = O.dihedrals(pos, s.box, t.dihedrals, s.dihedral_parameters)[0] \
+        if t.num_dihedrals else 0.0
+    return f_nb + (f_rec + f_ex + f_b + f_a + f_d)[sub]
+
+
+def sample_atoms(n, n_sample, seed=0):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, size=min(n_sample, n), replace=False))
+
+
+def rel_err(a, b):
+    return float(np.sqrt(np.sum((np.asarray(a) - b) ** 2) / np.sum(np.asarray(b) ** 2)))
+
+
+def applied_force_errors(s, sysm, mask, beta, k, n_sample=1000, seed=0, cutoff=CUTOFF,
+                         switch=SWITCH):
+    """Error of the force the integrator applies, step by step over one outer
+    cycle of k steps (k = 1: the plain form): after each step the device's
+    force buffer holds what the next half kick applies (the weighted
+    reciprocal term on an outer step, none on an impulse inner step, the
+    learned prediction between full evaluations); each is compared with the
+    FP64 force at that step's positions on sampled atoms.  Also the error of
+    the cycle-averaged force."""
+    sub = sample_atoms(s.num_particles, n_sample, seed)
+    while sysm.step % k:
+        sysm.integrate(1, mask, want_energy=False)
+    per, f_app, f_ref = [], [], []
+    t0 = time.perf_counter()
+    for _ in range(k):
+        sysm.integrate(1, mask, want_energy=False)
+        f = sysm.get_forces()[sub]
+        r = reference_forces(s, sysm.get_positions(), beta, sub, cutoff, switch)
+        per.append(rel_err(f, r))
+        f_app.append(f)
+        f_ref.append(r)
+    return {"per_step": per, "max": max(per), "cycle_average": rel_err(np.mean(f_app, 0),
+                                                                       np.mean(f_ref, 0)),
+            "sample_atoms": int(len(sub)), "outer_step": k,
+            "reference": "FP64: real space + PME %s order %d (0.5 A) + exclusions + bonded"
+                         % ("x".join(map(str, ref_pme_grid(s.box))), REF_PME_ORDER),
+            "wall_s": time.perf_counter() - t0}
 
 
 # --------------------------------------------------------------------------
 # CPU arm: the oracle port of the reference path, on the host cores
 # --------------------------------------------------------------------------
-def cpu_reference_sample(s, seconds):
-    """mdpy's CPU step restated by the oracle: LJ (cell list, hard cutoff 12 A)
-    + bare Coulomb over all pairs + bonds + angles + dihedrals per force
-    evaluation, three evaluations per Langevin step as mdpy's
-    LangevinIntegrator runs them (mdpy/integrator/langevin_integrator.py:51-64).
-    Times whole force evaluations on the full system until ``seconds`` pass."""
-    from oracle import oracle as O
+class ReferenceStep:
+    """mdpy's CPU step restated by the oracle (FP64 C port, all host threads):
+    per force evaluation LJ over the cell list (hard cutoff 12 A) + bare
+    Coulomb over all pairs (mdpy's ElectrostaticConstraint) + bonds + angles
+    (+ dihedrals), three evaluations per Langevin step as mdpy's
+    LangevinIntegrator runs them (mdpy/integrator/langevin_integrator.py:
+    51-64).  A sampled step evaluates the pair terms for a subset of the i
+    atoms (every m-th, rotating) and the bonded terms in full; the full step's
+    time is the pair time scaled by n / rows plus the bonded time."""
 
-    t = s.topology
-    n = s.num_particles
-    p = s.parameters["nonbonded"]
-    lj = np.array([[p[ty][0], p[ty][1], p[ty][0], p[ty][1]] for ty in t.particle_types])
-    q = t.charges.reshape(-1)
-    types = t.particle_types
-    kb = np.array([s.parameters["bond"]["%s-%s" % (types[i], types[j])] for i, j in t.bonds])
-    ka = np.array([s.parameters["angle"]["%s-%s-%s" % (types[i], types[j], types[k])]
-                   for i, j, k in t.angles])
-    threads = O.num_threads()
-    evals, t0 = 0, time.perf_counter()
-    while True:
-        te = time.perf_counter()
-        f1, _ = O.nonbonded(s.positions, s.box, lj, q, t.bonded_particles, t.scaling_particles,
-                            CUTOFF, coulomb="none")
-        f2, _ = O.nonbonded(s.positions, s.box, np.zeros((n, 4)), q, t.bonded_particles,
-                            t.scaling_particles, CUTOFF, lj=False, coulomb="bare")
-        O.bonds(s.positions, s.box, t.bonds, kb)
-        O.angles(s.positions, s.box, t.angles, ka)
+    def __init__(self, s):
+        from oracle import oracle as O
+
+        self.O = O
+        self.s = s
+        t = s.topology
+        p = s.parameters["nonbonded"]
+        self.lj = np.array([[p[ty][0], p[ty][1], p[ty][0], p[ty][1]] for ty in t.particle_types])
+        self.q = t.charges.reshape(-1)
+        self.kb, self.ka = _bonded_rows(s)
+        self.n = s.num_particles
+        self.threads = O.num_threads()
+
+    def pair_rows(self, rows):
+        O, s, t = self.O, self.s, self.s.topology
+        O.nonbonded(s.positions, s.box, self.lj, self.q, t.bonded_particles, t.scaling_particles,
+                    CUTOFF, coulomb="none", rows=rows)
+        O.nonbonded(s.positions, s.box, np.zeros((self.n, 4)), self.q, t.bonded_particles,
+                    t.scaling_particles, CUTOFF, lj=False, coulomb="bare", rows=rows)
+
+    def bonded(self):
+        O, s, t = self.O, self.s, self.s.topology
+        O.bonds(s.positions, s.box, t.bonds, self.kb)
+        O.angles(s.positions, s.box, t.angles, self.ka)
         if t.num_dihedrals:
             O.dihedrals(s.positions, s.box, t.dihedrals, s.dihedral_parameters)
-        evals += 1
-        if time.perf_counter() - t0 >= seconds or time.perf_counter() - te > seconds / 2:
-            break
-    per_eval = (time.perf_counter() - t0) / evals
-    per_step = 3.0 * per_eval
-    sps = 1.0 / per_step
+
+    def step(self, stride, offset):
+        """One sampled Langevin step: returns (seconds, extrapolated seconds
+        of the full step)."""
+        rows = np.arange(offset % stride, self.n, stride)
+        t_pair = t_bond = 0.0
+        for _ in range(3):
+            t0 = time.perf_counter()
+            self.pair_rows(rows)
+            t1 = time.perf_counter()
+            self.bonded()
+            t2 = time.perf_counter()
+            t_pair += t1 - t0
+            t_bond += t2 - t1
+        return t_pair + t_bond, t_pair * self.n / len(rows) + t_bond
+
+    def calibrate(self, seconds_per_step):
+        """Row stride m so that one sampled step takes about seconds_per_step."""
+        probe = max(64, self.n // 256)
+        rows = np.arange(0, self.n, max(1, self.n // probe))
+        t0 = time.perf_counter()
+        self.pair_rows(rows)
+        per_row = (time.perf_counter() - t0) / len(rows)
+        t0 = time.perf_counter()
+        self.bonded()
+        t_bond = time.perf_counter() - t0
+        budget = max(seconds_per_step / 3.0 - t_bond, per_row)
+        return max(1, int(math.ceil(self.n * per_row / budget)))
+
+
+def cpu_reference_sample(s, seconds):
+    """The CPU baseline beside the GPU arm: sampled reference steps for about
+    ``seconds`` of host time, extrapolated to whole steps."""
     from mdpy_gb300 import unit
 
+    ref = ReferenceStep(s)
+    stride = ref.calibrate(seconds / 4.0)
+    t_total, full = 0.0, []
+    k = 0
+    while t_total < seconds and k < 64:
+        dt, df = ref.step(stride, k)
+        t_total += dt
+        full.append(df)
+        k += 1
+    per_step = float(np.mean(full))
+    sps = 1.0 / per_step
     return {
         "ns_per_day": unit.ns_per_day(sps, DT_FS),
-        "atom_steps_per_s": n * sps,
-        "cores": threads,
+        "atom_steps_per_s": s.num_particles * sps,
+        "cores": ref.threads,
         "host_cores": os.cpu_count(),
-        "sample": ("%d full force evaluation(s) of the reference path (LJ cell list rc 12 A + "
-                   "bare Coulomb over all %d atom pairs + bonds/angles/dihedrals, FP64 C port, "
-                   "%d threads) on the %d-atom system; %.2f s per evaluation, x3 per Langevin "
-                   "step as mdpy runs it" % (evals, n, threads, n, per_eval)),
+        "sample": ("%d sampled Langevin steps of the reference path (FP64 C port, %d threads): "
+                   "per step 3 force evaluations of LJ (cell list, rc 12 A) + bare Coulomb over "
+                   "all atom pairs for every %d-th i atom (%d of %d), bonds/angles/dihedrals in "
+                   "full; %.3f s per sampled step, %.2f s per full step (pair time x %d)"
+                   % (k, ref.threads, stride, len(range(0, s.num_particles, stride)),
+                      s.num_particles, t_total / k, per_step, stride)),
     }
 
 
 # --------------------------------------------------------------------------
-# force error vs the FP64 oracle (a sample of atoms; structure factors use all)
-# --------------------------------------------------------------------------
-def force_error(s, ens, beta, n_sample=1000, seed=0):
-    from oracle import oracle as O
-
-    t = s.topology
-    n = s.num_particles
-    pos = ens.state.positions
-    ens.update()
-    f_gpu = ens.forces
-    p = s.parameters["nonbonded"]
-    lj = np.array([[p[ty][0], p[ty][1], p[ty][0], p[ty][1]] for ty in t.particle_types])
-    q = t.charges.reshape(-1)
-    rng = np.random.default_rng(seed)
-    sub = np.sort(rng.choice(n, size=min(n_sample, n), replace=False))
-    f_nb, _ = O.nonbonded(pos, s.box, lj, q, t.bonded_particles, t.scaling_particles, CUTOFF,
-                          switch=SWITCH, coulomb="ewald", beta=beta)
-    f_rec, _ = O.ewald_recip(pos, s.box, q, beta, O.ewald_kmax(s.box, beta, 1e-9), subset=sub)
-    f_ex, _ = O.ewald_exclusions(pos, s.box, q, t.bonded_particles, beta)
-    types = t.particle_types
-    kb = np.array([s.parameters["bond"]["%s-%s" % (types[i], types[j])] for i, j in t.bonds])
-    ka = np.array([s.parameters["angle"]["%s-%s-%s" % (types[i], types[j], types[k])]
-                   for i, j, k in t.angles])
-    f_b, _ = O.bonds(pos, s.box, t.bonds, kb)
-    f_a, _ = O.angles(pos, s.box, t.angles, ka)
-    f_d = O.dihedrals(pos, s.box, t.dihedrals, s.dihedral_parameters)[0] \
-        if t.num_dihedrals else 0.0
-    ref = (f_nb + f_ex + f_b + f_a + f_d)[sub] + f_rec
-    err = float(np.sqrt(np.sum((f_gpu[sub] - ref) ** 2) / np.sum(ref ** 2)))
-    return err, len(sub)
-
-
-# --------------------------------------------------------------------------
 def run_reference_arm(a, world, rank):
+    """The reference's CPU path on the host cores (rank 0 only): exactly
+    --warmup + --steps sampled Langevin steps (ReferenceStep), sized so that
+    they take about --reference-seconds together.  ms_per_step is the
+    measured time of a sampled step; value (ns/day) is the rate of whole
+    steps extrapolated from them."""
     if rank != 0:
         return 0
+    from mdpy_gb300 import unit
+
     s = make_system(a, seed=0)
-    r = cpu_reference_sample(s, a.cpu_seconds)
+    ref = ReferenceStep(s)
+    n_total = max(1, a.steps + a.warmup)
+    stride = ref.calibrate(a.reference_seconds / n_total)
+    for k in range(a.warmup):
+        ref.step(stride, k)
+    sample_s, full_s = [], []
+    for k in range(a.steps):
+        dt, df = ref.step(stride, a.warmup + k)
+        sample_s.append(dt)
+        full_s.append(df)
+    per_full = float(np.mean(full_s))
+    value = unit.ns_per_day(1.0 / per_full, DT_FS)
+    rows = len(range(0, s.num_particles, stride))
+    sample = ("each step: one sampled Langevin step of the reference path (FP64 C port of "
+              "mdpy's CPU kernels, %d threads): 3 force evaluations of LJ (cell list, rc 12 A) + "
+              "bare Coulomb over all atom pairs for every %d-th i atom (%d of %d, rotating), "
+              "bonds/angles/dihedrals in full; value and atom_steps_per_s are whole steps "
+              "extrapolated (pair time x %d + bonded time = %.3f s per full step); ms_per_step "
+              "is the measured sampled step" % (ref.threads, stride, rows, s.num_particles,
+                                                stride, per_full))
     line = {
-        "metric": METRIC, "value": r["ns_per_day"], "unit": "ns/day", "impl": "reference",
+        "metric": METRIC, "value": value, "unit": "ns/day", "impl": "reference",
         "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": 1000.0 * s.num_particles / r["atom_steps_per_s"],
+        "ms_per_step": 1000.0 * float(np.mean(sample_s)),
+        "ms_per_full_step_extrapolated": 1000.0 * per_full,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "atom_steps_per_s": r["atom_steps_per_s"],
+        "data": "synthetic", "atom_steps_per_s": s.num_particles / per_full,
         "config": {"workload": workload_name(a, s.num_particles), "atoms": s.num_particles,
-                   "l2": "n/a (host)"},
-        "cpu_baseline": {"value": r["ns_per_day"], "unit": "ns/day", "cores": r["cores"],
-                         "kind": "port", "sample": r["sample"]},
-        "e2e": {"value": r["ns_per_day"], "unit": "ns/day", "h2d_bytes_per_step": 0,
+                   "replicas": 1, "l2": "n/a (host)",
+                   "precision": "f64 (FP64 C port of mdpy's float32 CPU kernels)",
+                   "form": "reference CPU path: LJ cell list + all-pairs bare Coulomb + bonded, "
+                           "3 force evaluations per Langevin step",
+                   "launch_shape": None, "sampled": sample},
+        "cpu_baseline": {"value": value, "unit": "ns/day", "cores": ref.threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "ns/day", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -560,6 +783,68 @@ def profile_learned(a):
     out["judge"] = sysm.learned_stats()
     print(json.dumps(out))
     return 0
+
+
+def pair_kernel_roofline(stats, t_nb, n, clk, device):
+    """The pair kernel against each limit that could bind it: HBM bytes,
+    warp-instruction issue and FP32 throughput.  ``bound`` names the limit
+    with the largest fraction; the others are kept beside it."""
+    import torch
+
+    n_pad = 32 * ((n + 31) // 32)
+    # algorithmic bytes: coordinates+charge (16 B) + LJ parameters (8 B) read
+    # once and three int64 force words (24 B) written once per atom slot, plus
+    # the cluster box and partner range (40 B per cluster)
+    alg_bytes = 48 * n_pad + 40 * (n_pad // 32)
+    peaks = {}
+    if os.path.exists(PEAKS):
+        with open(PEAKS) as fh:
+            peaks = json.load(fh)
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    sm_mhz = None
+    try:
+        sm_mhz = float(clk.get("sm_mhz")) if clk and clk.get("sm_mhz") else None
+    except (TypeError, ValueError):
+        sm_mhz = None
+    sm_mhz = sm_mhz or 2070.0
+    n_sms = torch.cuda.get_device_properties(device).multi_processor_count
+    traffic, issue = None, None
+    if os.path.exists(PROFILE_INPUTS):
+        with open(PROFILE_INPUTS) as fh:
+            prof = json.load(fh)
+        # one ncu capture of the 88k box; other sizes scale by the units processed
+        traffic = prof["nonbonded_dram_bytes_per_launch"] * alg_bytes / prof["alg_bytes_per_launch"]
+        inst = (prof["warp_instructions_per_launch"] * stats["pair_evaluations"]
+                / prof["pair_evaluations_per_launch"])
+        peak_issue = n_sms * 4 * sm_mhz * 1e6   # 4 schedulers per SM, 1 instruction/clock each
+        issue = {"achieved": inst / t_nb / 1e9, "peak": peak_issue / 1e9,
+                 "unit": "G warp instructions/s", "frac": inst / t_nb / peak_issue,
+                 "warp_instructions_per_launch": inst,
+                 "source": "instructions per pair evaluation from the ncu capture in "
+                           "profiles/roofline_inputs.json x this launch's evaluations; peak = "
+                           "SMs x 4 schedulers x sampled SM clock"}
+    achieved = alg_bytes / t_nb / 1e9
+    fp32_peak = n_sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+    flops = 60.0 * stats["pairs_in_cutoff"] / t_nb / 1e12
+    hbm = {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+           "traffic": traffic, "peak_source": peak_src, "alg_bytes_per_launch": alg_bytes}
+    fp32 = {"achieved": flops, "peak": fp32_peak, "unit": "TFLOP/s", "frac": flops / fp32_peak,
+            "flops_per_pair": 60, "pairs_in_cutoff": stats["pairs_in_cutoff"],
+            "pair_evaluations": stats["pair_evaluations"],
+            "useful_pair_fraction": stats["pairs_in_cutoff"] / max(1, stats["pair_evaluations"]),
+            "peak_source": "SMs x 128 FP32 lanes x FMA x sampled SM clock"}
+    limits = {"hbm": hbm, "fp32": fp32}
+    if issue is not None:
+        limits["issue"] = issue
+    bound = max(limits, key=lambda k: limits[k]["frac"])
+    top = limits[bound]
+    out = {"bound": bound, "achieved": top["achieved"], "peak": top["peak"], "unit": top["unit"],
+           "frac": top["frac"], "traffic": traffic, "kernel": "k_nonbonded",
+           "launch_ms": t_nb * 1e3, "fractions": {k: v["frac"] for k, v in limits.items()}}
+    out.update(limits)
+    return out
 
 
 def main():
@@ -649,91 +934,15 @@ def main():
     sysm.set_positions(x_save)
     sysm.set_velocities(v_save)
     ens.update()  # a valid force buffer again
-
-    # pair-kernel roofline: algorithmic bytes = coordinates+charge (16 B) +
-    # LJ parameters (8 B) read once and three int64 force words (24 B) written
-    # once per atom, plus the cluster box and partner range (40 B per cluster)
-    n_pad = 32 * ((n + 31) // 32)
-    alg_bytes = 48 * n_pad + 40 * (n_pad // 32)
-    t_nb = stage_ms["nonbonded"] * 1e-3
-    peaks = {}
-    if os.path.exists(PEAKS):
-        with open(PEAKS) as fh:
-            peaks = json.load(fh)
-    hbm_peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if hbm_peak else "fallback"
-    hbm_peak = hbm_peak or 6800.0
-    traffic = None
-    issue = None
-    pairs_in = stats["pairs_in_cutoff"]
-    if os.path.exists(PROFILE_INPUTS):
-        with open(PROFILE_INPUTS) as fh:
-            prof = json.load(fh)
-        # one ncu capture of the 88k box; other sizes scale by the units processed
-        traffic = prof["nonbonded_dram_bytes_per_launch"] * alg_bytes / prof["alg_bytes_per_launch"]
-        inst = (prof["warp_instructions_per_launch"] * stats["pair_evaluations"]
-                / prof["pair_evaluations_per_launch"])
-        # the binding limit of this kernel: warp-instruction issue (4 schedulers
-        # per SM, one instruction per clock each) at the sampled SM clock
-        sm_mhz = None
-        try:
-            sm_mhz = float(clk.get("sm_mhz")) if clk and clk.get("sm_mhz") else None
-        except (TypeError, ValueError):
-            sm_mhz = None
-        sm_mhz = sm_mhz or 2070.0
-        n_sms = torch.cuda.get_device_properties(local).multi_processor_count
-        peak_issue = n_sms * 4 * sm_mhz * 1e6
-        issue = {"warp_instructions_per_launch": inst, "achieved_per_s": inst / t_nb,
-                 "peak_per_s": peak_issue, "frac": inst / t_nb / peak_issue,
-                 "source": "instructions per pair evaluation from the ncu capture in "
-                           "profiles/roofline_inputs.json x this launch's evaluations; "
-                           "peak = SMs x 4 schedulers x sampled SM clock"}
-    achieved = alg_bytes / t_nb / 1e9
-    flops = 60.0 * pairs_in / t_nb / 1e12
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": traffic, "kernel": "k_nonbonded",
-                "peak_source": peak_src, "alg_bytes_per_launch": alg_bytes,
-                "launch_ms": stage_ms["nonbonded"],
-                "issue": issue,
-                "fp32": {"achieved_tflops": flops, "nominal_peak_tflops": FP32_PEAK_TFLOPS_NOMINAL,
-                         "frac": flops / FP32_PEAK_TFLOPS_NOMINAL,
-                         "flops_per_pair": 60, "pairs_in_cutoff": pairs_in,
-                         "pair_evaluations": stats["pair_evaluations"]}}
+    roofline = pair_kernel_roofline(stats, stage_ms["nonbonded"] * 1e-3, n, clk, local)
 
     # ---- end to end through the public API with pinned host buffers --------
-    x_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
-    v_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
-    sysm.get_positions_ptr(x_h.data_ptr(), _lib.HOST)
-    sysm.get_velocities_ptr(v_h.data_ptr(), _lib.HOST)
-    torch.cuda.synchronize()
-    barrier(world)
-    t0 = time.perf_counter()
-    e_terms = np.zeros(_lib.NUM_TERMS)
-    for k in range(a.e2e_steps):
-        # one C-ABI call: host state in, one step, host state and energies out
-        sysm.step_host_ptr(x_h.data_ptr(), v_h.data_ptr(), 1, mask, x_h.data_ptr(),
-                           v_h.data_ptr(), e_terms)
-    torch.cuda.synchronize()
-    e2e_s = reduce_max(time.perf_counter() - t0, world,
-                       device=torch.device("cuda", local)
-                       if world > 1 and os.environ.get("MDG_BENCH_BACKEND", "nccl") == "nccl"
-                       else None)
-    e2e_value = unit.ns_per_day(world * a.e2e_steps / e2e_s, DT_FS)
-    e2e = {"value": e2e_value, "unit": "ns/day", "h2d_bytes_per_step": 2 * n * 24,
-           "d2h_bytes_per_step": 2 * n * 24 + 8 * (_lib.NUM_TERMS + 1) + 4,
-           "api": "mdg_step_host: positions + velocities in from pinned host memory (the "
-                  "previous call's outputs), one step, wrapped positions + velocities + "
-                  "energies out; the incoming positions are compared on the device with the "
-                  "state (one 4-byte read and a synchronisation), and equal ones keep their "
-                  "forces and cluster order -- other positions trigger a re-sort and a fresh "
-                  "force evaluation"}
+    e2e = end_to_end(sysm, mask, n, a, world, local)
 
     # what a multiple-time-step scheme could save at most: the same step
     # with the reciprocal-space term left out (PME runs beside the pair
     # kernel on the side stream, so only its share of the SMs shows)
-    from mdpy_gb300 import _lib as L_
-
-    no_pme = mask & ~L_.mask(L_.TERM_COUL_RECIP)
+    no_pme = mask & ~_lib.mask(_lib.TERM_COUL_RECIP)
     sysm.integrate(5, no_pme, want_energy=False)
     reps = max(50, a.steps // 4)
     ms_no_pme = time_steps(sysm, no_pme, reps, stream, flush) / reps
@@ -791,55 +1000,79 @@ def main():
         forms.append(f)
         learned_forms[id(f)] = lrn
 
-    # every NVE run starts from the same state, and the state is put back
-    # afterwards (a form whose run diverges must not spoil what follows)
-    x_keep, v_keep = sysm.get_positions(), sysm.get_velocities()
+    plain = {"form": "plain", "ns_per_day": value, "atom_steps_per_s": n * sps_job,
+             "ms_per_step": ms_step}
 
-    def restore():
-        sysm.set_mts(1)
+    # ---- force error of every form against FP64 (rank 0; the oracle is host
+    # code): the force each form applies, step by step over one outer cycle,
+    # from the same state
+    if rank == 0 and world == 1 and not a.no_error_check:
+        x_keep, v_keep = sysm.get_positions(), sysm.get_velocities()
+        for f in [plain] + forms:
+            sysm.set_positions(x_keep)
+            sysm.set_velocities(v_keep)
+            sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 4244)
+            lrn = learned_forms.get(id(f))
+            k = f.get("mts", f.get("learned", 1))
+            if lrn is not None:
+                lrn.enable(sysm)
+                sysm.integrate(2 * k, mask, want_energy=False)   # past the first anchor
+            else:
+                sysm.set_mts(k)
+            try:
+                f["force_error"] = applied_force_errors(s, sysm, mask, beta, k)
+            finally:
+                sysm.set_mts(1)
+        sysm.set_positions(x_keep)
+        sysm.set_velocities(v_keep)
+
+    # ---- NVE drift: one shared Langevin equilibration, then every form from
+    # the same equilibrated state (a form whose run diverges is a result)
+    if a.nve_ps > 0:
+        x_keep, v_keep = sysm.get_positions(), sysm.get_velocities()
+        t_eq = time.perf_counter()
+        equilibrate(sysm, mask, a.equilibrate_ps)
+        t_eq = time.perf_counter() - t_eq
+        x_eq, v_eq = sysm.get_positions(), sysm.get_velocities()
+        for f in [plain] + forms:
+            sysm.set_positions(x_eq)
+            sysm.set_velocities(v_eq)
+            try:
+                f["nve_drift"] = nve_drift(sysm, mask, n, a.nve_ps, mts=f.get("mts", 1),
+                                           learned=learned_forms.get(id(f)))
+                f["nve_drift"]["equilibration"] = "%g ps Langevin at 300 K (%.0f s), shared" % (
+                    a.equilibrate_ps, t_eq)
+            except Exception as e:  # noqa: BLE001 -- a diverging form is a result
+                f["nve_drift"] = {"diverged": "%s: %s" % (type(e).__name__, e),
+                                  "kT_per_ns_per_atom": None, "stderr_kT_per_ns_per_atom": None}
+            finally:
+                sysm.set_mts(1)
         sysm.set_positions(x_keep)
         sysm.set_velocities(v_keep)
         sysm.integrator_config(_lib.INTEGRATOR_LANGEVIN, DT_FS, TEMPERATURE, FRICTION, 4243)
 
-    def drift_of(**kw):
-        try:
-            return nve_drift(sysm, mask, n, a.nve_ps, **kw)
-        except Exception as e:  # noqa: BLE001 -- a diverging form is a result
-            return {"diverged": "%s: %s" % (type(e).__name__, e),
-                    "kT_per_ns_per_atom": None, "stderr_kT_per_ns_per_atom": None}
-        finally:
-            restore()
-
-    nve = drift_of() if a.nve_ps > 0 else None
-    if a.nve_ps > 0:
-        for f in forms:
-            f["nve_drift"] = drift_of(mts=f.get("mts", 1), seed=1,
-                                      learned=learned_forms.get(id(f)))
-
-    err = None
     cpu = None
-    if rank == 0 and world == 1:
-        if not a.no_error_check:
-            err, nsub = force_error(s, ens, beta)
-        if not a.no_cpu_baseline:
-            r = cpu_reference_sample(s, a.cpu_seconds)
-            cpu = {"value": r["ns_per_day"], "unit": "ns/day", "cores": r["cores"],
-                   "kind": "port", "sample": r["sample"],
-                   "atom_steps_per_s": r["atom_steps_per_s"]}
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        r = cpu_reference_sample(s, a.cpu_seconds)
+        cpu = {"value": r["ns_per_day"], "unit": "ns/day", "cores": r["cores"],
+               "kind": "port", "sample": r["sample"],
+               "atom_steps_per_s": r["atom_steps_per_s"]}
 
     if rank == 0:
-        plain = {"form": "plain", "ns_per_day": value, "atom_steps_per_s": n * sps_job,
-                 "ms_per_step": ms_step, "nve_drift": nve}
-        # the chosen form: the fastest whose NVE drift (when measured) is not
-        # shown to exceed 1e-3 kT/ns/atom (|drift| - 2 standard errors)
-        def within(f):
-            d = f.get("nve_drift")
-            if d is None:
-                return True
-            if d.get("kT_per_ns_per_atom") is None:  # the run diverged
-                return False
-            return abs(d["kT_per_ns_per_atom"]) - 2 * d["stderr_kT_per_ns_per_atom"] <= 1e-3
-        chosen = max([plain] + [f for f in forms if within(f)], key=lambda f: f["ns_per_day"])
+        # gates: the applied per-step force error (largest over one outer
+        # cycle) within FORCE_BAR of FP64, and |NVE drift| + 2 sigma within
+        # DRIFT_BAR; a gate that was not measured on this run is reported as
+        # such and does not pass
+        def gates(f):
+            fe = f.get("force_error")
+            g = {"force": None if fe is None else fe["max"] <= FORCE_BAR,
+                 "drift": None if a.nve_ps <= 0 else drift_passes(f.get("nve_drift"))}
+            f["gates"] = g
+            return all(v is True for v in g.values() if v is not None) and g["force"] is True
+
+        passing = [f for f in [plain] + forms if gates(f)]
+        chosen = max(passing, key=lambda f: f["ns_per_day"]) if passing else None
+        err = plain.get("force_error", {}).get("max") if plain.get("force_error") else None
         line = {
             "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_step,
@@ -852,9 +1085,16 @@ def main():
                        "form": "plain", "launch_shape": shape},
             "atom_steps_per_s": n * sps_job,
             "force_rel_rms_err_vs_fp64": err,
-            "nve_drift": nve,
+            "gates": {"force_rel_rms_max_over_cycle": FORCE_BAR,
+                      "nve_drift_kT_per_ns_per_atom": DRIFT_BAR,
+                      "drift_rule": "|drift| + 2 standard errors <= bar"},
             "mts_bound": mts_bound,
-            "plain": plain, "chosen": chosen, "forms": forms,
+            "plain": plain, "forms": forms,
+            "chosen": ({"form": chosen["form"], "ns_per_day": chosen["ns_per_day"],
+                        "atom_steps_per_s": chosen["atom_steps_per_s"],
+                        "ms_per_step": chosen["ms_per_step"]}
+                       if chosen else None),
+            "chosen_note": None if chosen else "no form passed both gates on this run",
             "roofline": roofline, "stages_ms": stage_ms, "nonbonded_stats": stats,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clk,
@@ -865,6 +1105,62 @@ def main():
 
         dist.destroy_process_group()
     return 0
+
+
+def end_to_end(sysm, mask, n, a, world, local):
+    """The metric through the public C ABI with host buffers: every step one
+    mdg_step_host call copies positions + velocities in from pinned host
+    memory (the previous call's outputs), runs one step and copies the
+    wrapped positions, the velocities and the energies out.  Also the same
+    loop with the energies read every 10th step (LogDumper style), and the
+    device-only step of the same graph mode for the breakdown."""
+    import torch
+
+    from mdpy_gb300 import _lib, unit
+
+    dev = torch.device("cuda", local) if world > 1 and \
+        os.environ.get("MDG_BENCH_BACKEND", "nccl") == "nccl" else None
+    x_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    v_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    sysm.get_positions_ptr(x_h.data_ptr(), _lib.HOST)
+    sysm.get_velocities_ptr(v_h.data_ptr(), _lib.HOST)
+    e_terms = np.zeros(_lib.NUM_TERMS)
+
+    def loop(steps, energy_every):
+        for k in range(steps):
+            want = (k + 1) % energy_every == 0
+            sysm.step_host_ptr(x_h.data_ptr(), v_h.data_ptr(), 1, mask, x_h.data_ptr(),
+                               v_h.data_ptr(), e_terms if want else None)
+
+    out = {}
+    for name, every in (("energies_every_step", 1), ("energies_every_10_steps", 10)):
+        loop(5, every)   # warm-up: graphs of this variant
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        loop(a.e2e_steps, every)
+        torch.cuda.synchronize()
+        dt = reduce_max(time.perf_counter() - t0, world, device=dev)
+        out[name] = {"ns_per_day": unit.ns_per_day(world * a.e2e_steps / dt, DT_FS),
+                     "ms_per_step": 1000.0 * dt / a.e2e_steps}
+    # the same steps without the host copies (device state, one synchronise)
+    for name, want in (("device_step_with_energies", True), ("device_step", False)):
+        sysm.integrate(5, mask, want_energy=want)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.e2e_steps):
+            sysm.integrate(1, mask, want_energy=want)
+        torch.cuda.synchronize()
+        out[name] = {"ms_per_step": 1000.0 * (time.perf_counter() - t0) / a.e2e_steps}
+    head = out["energies_every_step"]
+    return {"value": head["ns_per_day"], "unit": "ns/day", "h2d_bytes_per_step": 2 * n * 24,
+            "d2h_bytes_per_step": 2 * n * 24 + 8 * (_lib.NUM_TERMS + 1) + 4,
+            "api": "mdg_step_host: positions + velocities in from pinned host memory (the "
+                   "previous call's outputs), one step, wrapped positions + velocities + "
+                   "energies out, one synchronisation; the incoming positions are compared on "
+                   "the device with the state while the step runs on it, and the step is redone "
+                   "from a re-sort and a fresh force evaluation if they differ",
+            "breakdown": out}
 
 
 if __name__ == "__main__":

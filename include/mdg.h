@@ -5,7 +5,7 @@
  * The reference (mdpy v0.2.1) is pure Python and has no FFI; each entry point
  * below names the reference interface whose work it takes over (paths are
  * relative to the mdpy source tree).  The Python host layer in
- * mdpy_gb300/ binds these through ctypes (see INTEGRATION.md).
+ * mdpy_gb300/ binds these through ctypes.
  *
  * Conventions
  *  - Every function returns an int status: MDG_OK (0) or an MDG_ERR_* code.
@@ -41,7 +41,8 @@ extern "C" {
 #define MDG_ERR_NOMEM 3         /* device allocation failed */
 #define MDG_ERR_BOX 4           /* box not orthorhombic / not positive */
 #define MDG_ERR_CUTOFF 5        /* cutoff >= half the box (minimum image breaks) */
-#define MDG_ERR_PARTICLE_LOSS 6 /* non-finite position or velocity */
+#define MDG_ERR_PARTICLE_LOSS 6 /* non-finite position or velocity, or a position
+                                   two or more box lengths from the central image */
 #define MDG_ERR_OVERFLOW 7      /* fixed-point force/energy overflow */
 #define MDG_ERR_CUFFT 8         /* cuFFT failure */
 #define MDG_ERR_TIMEOUT 9       /* a bounded device wait gave up */
@@ -315,6 +316,16 @@ MDG_API int mdg_set_mts_learned(mdg_system *sys, int32_t k, double threshold);
 MDG_API int mdg_learned_set_terms(mdg_system *sys, int32_t field_gradient, int32_t network);
 /* 1: the tcgen05 tensor-core MLP kernel for inference; 0: the SIMT kernel */
 MDG_API int mdg_learned_set_kernel(mdg_system *sys, int32_t tensor_cores);
+/* Test of the tcgen05 inference kernel's bounded waits (no reference
+ * counterpart).  Arms a one-shot test: the next launch of that kernel
+ * withholds its first bulk copy (weights and first feature tile), so its
+ * first mbarrier wait gives up after 10 ms of wall time instead of the
+ * usual 1 s.  The kernel then raises MDG_ERR_TIMEOUT, has no MMA and no copy
+ * in flight to wait for, frees its tensor memory and returns; the call that
+ * launched it (e.g. mdg_learned_predict) returns MDG_ERR_TIMEOUT and the
+ * system stays usable.  MDG_ERR_STATE unless the tensor-core kernel is
+ * selected. */
+MDG_API int mdg_learned_wait_test(mdg_system *sys);
 /* out[8]: last judged error, largest, sum of errors, judgements, fallbacks,
  * last training loss, last training target norm, mode of the current
  * interval (0 learned, 1 impulse fallback) */

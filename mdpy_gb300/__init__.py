@@ -21,7 +21,7 @@ def __getattr__(name):
     if name == "Simulation":
         from .simulation import Simulation
         return Simulation
-    if name in ("SteepestDescentMinimizer", "ConjugateGradientMinimizer"):
+    if name == "SteepestDescentMinimizer":
         from . import minimizer
         return getattr(minimizer, name)
     if name == "EnsembleBatch":
@@ -38,6 +38,6 @@ def __getattr__(name):
 
 
 __all__ = ["unit", "error", "Particle", "Topology", "Ensemble", "State", "Simulation",
-           "SteepestDescentMinimizer", "ConjugateGradientMinimizer", "EnsembleBatch",
+           "SteepestDescentMinimizer", "EnsembleBatch",
            "LearnedSlowForce", "constraint", "integrator", "simulation", "systems", "minimizer",
            "batch", "forcefield", "learned"]

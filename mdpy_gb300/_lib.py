@@ -87,6 +87,7 @@ SIGNATURES = {
     "mdg_learned_predict": [_sys_p, ctypes.c_int32, _c_f32_p],
     "mdg_set_mts_learned": [_sys_p, ctypes.c_int32, ctypes.c_double],
     "mdg_learned_set_kernel": [_sys_p, ctypes.c_int32],
+    "mdg_learned_wait_test": [_sys_p],
     "mdg_learned_set_terms": [_sys_p, ctypes.c_int32, ctypes.c_int32],
     "mdg_learned_stats": [_sys_p, _c_dbl_p],
     "mdg_learned_reset_stats": [_sys_p],
@@ -420,6 +421,11 @@ class System:
 
     def learned_set_kernel(self, tensor_cores):
         check(self._lib.mdg_learned_set_kernel(self._h, int(bool(tensor_cores))))
+
+    def learned_wait_test(self):
+        """Arm the one-shot test of the tcgen05 kernel's bounded waits (its
+        next launch gives up on its first wait and reports a timeout)."""
+        check(self._lib.mdg_learned_wait_test(self._h))
 
     def learned_set_terms(self, field_gradient=True, network=True):
         check(self._lib.mdg_learned_set_terms(self._h, int(bool(field_gradient)),

@@ -141,7 +141,8 @@ int decode_status(mdg_system *s, int st) {
             if (st & (1 << code)) {
                 switch (code) {
                     case MDG_ERR_PARTICLE_LOSS:
-                        return fail(code, "non-finite position or velocity");
+                        return fail(code, "non-finite position or velocity, or a position two "
+                                          "or more box lengths from the central image");
                     case MDG_ERR_OVERFLOW:
                         return fail(code, "force or energy beyond the int64 fixed-point range");
                     default:
@@ -554,6 +555,7 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     if (s->host_stage) cudaFreeHost(s->host_stage);
     dfree(s->xin);
+    dfree(s->vsave);
     dfree(s->same_flag);
     delete s;
     return MDG_OK;
@@ -1308,31 +1310,55 @@ MDG_API int mdg_step_host(mdg_system *s, const double *x_in, const double *v_in,
     int rc = check_sys(s);
     if (rc) return rc;
     const size_t ne = (size_t)kEnergySlots * s->n_sys;
-    if (!s->host_stage) {
+    if (!s->host_stage || !s->xin || !s->same_flag) {
         // pinned staging for the energy words, the status word and the
-        // positions-comparison flag
-        CK(cudaMallocHost((void **)&s->host_stage, sizeof(long long) * (ne + 2)),
-           "pinned staging");
-        int rc2 = dalloc(&s->xin, 3 * (size_t)s->n);
-        if (!rc2) rc2 = dalloc(&s->same_flag, 1);
+        // positions-comparison flag; each buffer is allocated once, so a
+        // failed call leaves nothing half set up for the next one
+        if (!s->host_stage)
+            CK(cudaMallocHost((void **)&s->host_stage, sizeof(long long) * (ne + 2)),
+               "pinned staging");
+        int rc2 = s->xin ? 0 : dalloc(&s->xin, 3 * (size_t)s->n);
+        if (!rc2 && !s->same_flag) rc2 = dalloc(&s->same_flag, 1);
         if (rc2) return fail(rc2, "step_host staging");
     }
+    long long *stage = s->host_stage;
+    // Positions that equal the state (as the previous call returned it) keep
+    // the forces already computed for them and the cluster order.  The copy
+    // lands beside the state and a comparison kernel flags any difference;
+    // the steps run on the device state meanwhile (speculatively), and the
+    // flag comes back with the results.  If the positions differed, the
+    // state before the call is put back and the call is redone from the
+    // incoming positions (re-sort, fresh force evaluation).  A learned slow
+    // force keeps more state than positions and velocities: there the flag
+    // is read before the steps.
+    bool speculate = false;
+    const uint64_t step0 = s->step;
+    const int since0 = s->steps_since_reorder;
     if (x_in) {
-        // Positions that equal the state (as the previous call returned it)
-        // keep the forces already computed for them, and the cluster order:
-        // the copy lands beside the state and one comparison decides.
-        bool same = false;
         CK(cudaMemcpyAsync(s->xin, x_in, sizeof(double) * 3 * s->n, cudaMemcpyHostToDevice,
                            s->stream),
            "copy positions");
+        bool same = false;
         if (s->have_x && s->forces_valid) {
             CK(cudaMemsetAsync(s->same_flag, 0, sizeof(int), s->stream), "memset");
             CK(launch_same_positions(s, s->xin, s->same_flag), "compare positions");
-            CK(cudaMemcpyAsync(s->host_stage + ne + 1, s->same_flag, sizeof(int),
-                               cudaMemcpyDeviceToHost, s->stream),
-               "flag read");
-            CK(cudaStreamSynchronize(s->stream), "synchronize");
-            same = ((int)(s->host_stage[ne + 1] & 0xffffffffll)) == 0;
+            if (!ls_active(s)) {
+                if (!v_in) {  // the velocities to restore should the step be redone
+                    if (!s->vsave && (rc = dalloc(&s->vsave, 3 * (size_t)s->n)))
+                        return fail(rc, "step_host staging");
+                    CK(cudaMemcpyAsync(s->vsave, s->v, sizeof(double) * 3 * s->n,
+                                       cudaMemcpyDeviceToDevice, s->stream),
+                       "save velocities");
+                }
+                speculate = true;
+                same = true;
+            } else {
+                CK(cudaMemcpyAsync(stage + ne + 1, s->same_flag, sizeof(int),
+                                   cudaMemcpyDeviceToHost, s->stream),
+                   "flag read");
+                CK(cudaStreamSynchronize(s->stream), "synchronize");
+                same = ((int)(stage[ne + 1] & 0xffffffffll)) == 0;
+            }
         }
         if (!same) {
             CK(cudaMemcpyAsync(s->x, s->xin, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToDevice,
@@ -1365,14 +1391,31 @@ MDG_API int mdg_step_host(mdg_system *s, const double *x_in, const double *v_in,
         CK(cudaMemcpyAsync(v_out, s->v, sizeof(double) * 3 * s->n, cudaMemcpyDeviceToHost,
                            s->stream),
            "copy velocities");
-    long long *stage = s->host_stage;
     if (want_energy)
         CK(cudaMemcpyAsync(stage, s->energy, sizeof(long long) * ne, cudaMemcpyDeviceToHost,
                            s->stream),
            "copy energies");
     CK(cudaMemcpyAsync(stage + ne, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
        "status read");
+    if (speculate)
+        CK(cudaMemcpyAsync(stage + ne + 1, s->same_flag, sizeof(int), cudaMemcpyDeviceToHost,
+                           s->stream),
+           "flag read");
     CK(cudaStreamSynchronize(s->stream), "synchronize");
+    if (speculate && (int)(stage[ne + 1] & 0xffffffffll) != 0) {
+        // the positions differed: the speculative steps and anything they
+        // raised are void; back to the state before the call, then redo
+        // from the incoming positions
+        CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
+        if (!v_in)
+            CK(cudaMemcpyAsync(s->v, s->vsave, sizeof(double) * 3 * s->n,
+                               cudaMemcpyDeviceToDevice, s->stream),
+               "restore velocities");
+        s->step = step0;
+        s->steps_since_reorder = since0;
+        s->forces_valid = 0;  // the redo takes the incoming positions as new
+        return mdg_step_host(s, x_in, v_in, n_steps, mask, x_out, v_out, energies, kinetic);
+    }
     const int st = (int)(stage[ne] & 0xffffffffll);
     if (st) {
         CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream), "status clear");
@@ -1581,6 +1624,15 @@ MDG_API int mdg_learned_set_kernel(mdg_system *s, int32_t tensor_cores) {
     if (rc) return rc;
     s->ls->use_tc = tensor_cores ? 1 : 0;
     drop_graph(s);
+    return MDG_OK;
+}
+
+MDG_API int mdg_learned_wait_test(mdg_system *s) {
+    int rc = ls_check(s);
+    if (rc) return rc;
+    if (!s->ls->use_tc) return fail(MDG_ERR_STATE, "the tensor-core kernel is not selected");
+    s->ls->tc_wait_test = 1;
+    drop_graph(s);  // the next launch must be an eager one
     return MDG_OK;
 }
 

@@ -163,6 +163,34 @@ struct SysDev {
     long long cgrid_off;    // offset of its complex grid and influence function
 };
 
+// Pair-set parity mode (the pair dump only): the reference's own pair test
+// in its float32 arithmetic.  The FP64 state is first put in the reference's
+// frame by mdpy's wrap (x - L round(x / L) with the float32 inverse box,
+// mdpy/utils/pbc.py:28-36 -- the positions mdg_get_positions reports) and
+// rounded to float32 (mdpy's positions are float32); then d
+// = x_j - x_i, scaled by the float32 inverse box, minus its rounded value,
+// scaled back (unwrap_vec, pbc.py:38-43), and r = sqrt of the left-to-right
+// sum of squares (np.linalg.norm, charmm_nonbonded_constraint.py:85-90),
+// every operation rounded once (no fused multiply-add), compared with rc.
+__device__ __forceinline__ bool ref_within32(const double *x, int i, int j, const SysDev &sd,
+                                             float rc) {
+    float d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double Ld = sd.Ld[k];
+        const double inv32 = (double)(float)(1.0 / Ld);
+        const double xi = x[3 * i + k] - Ld * rint(x[3 * i + k] * inv32);
+        const double xj = x[3 * j + k] - Ld * rint(x[3 * j + k] * inv32);
+        const float L = (float)Ld;
+        float sc = __fmul_rn(__fsub_rn((float)xj, (float)xi), __frcp_rn(L));
+        sc = __fsub_rn(sc, rintf(sc));
+        d[k] = __fmul_rn(sc, L);
+    }
+    const float r2 =
+        __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2]));
+    return __fsqrt_rn(r2) <= rc;
+}
+
 // systems sharing one PME grid size: one batched cuFFT plan pair
 struct PmeGroup {
     int K[3];
@@ -321,6 +349,8 @@ struct Learned {
     int use_tc = 1;            // tensor-core (tcgen05) inference kernel (0: SIMT)
     int use_taylor = 0;        // field-gradient term J (x - x0) in the prediction
     int use_net = 1;           // the network's G(x) - G(x0) in the prediction
+    int tc_wait_test = 0;      // one-shot test of the tcgen05 kernel's bounded waits (see
+                               // mdg_learned_wait_test)
     int *cell_of = nullptr, *cell_count = nullptr, *cell_start = nullptr,
         *cell_cursor = nullptr, *cell_atoms = nullptr;
     int *nlist = nullptr, *list = nullptr;  // per slot of the cell order; list: [cap][n]
@@ -424,6 +454,7 @@ struct mdg_system {
     double *fout = nullptr;            // (n,3) FP64 staging for get_forces
     long long *host_stage = nullptr;   // pinned host staging of mdg_step_host
     double *xin = nullptr;             // mdg_step_host: incoming positions (3n)
+    double *vsave = nullptr;           // and the velocities before a speculative step
     int *same_flag = nullptr;          // and their comparison with the state
 
     // launch shapes (set by hand or by mdg_autotune): work items per

@@ -22,9 +22,10 @@
 // The weight images and each tile's features (stored in this layout by the
 // feature kernel) arrive by bulk copies (cp.async.bulk) on a second
 // mbarrier; the next tile's features load while the current tile's
-// epilogues run.  Every mbarrier wait is bounded; a wait that gives up
-// raises MDG_ERR_TIMEOUT, waits (bounded) for the MMAs and copies in flight,
-// frees the tensor memory and leaves.
+// epilogues run.  Every mbarrier wait is bounded by wall time (1 s on the
+// GPU's global timer); a wait that gives up raises MDG_ERR_TIMEOUT, waits
+// (bounded the same way) for the MMAs and copies it started and has not
+// seen complete, frees the tensor memory and leaves.
 #include <cuda_bf16.h>
 
 #include "mdg_internal.cuh"
@@ -107,8 +108,23 @@ __device__ __forceinline__ void expect_tx(uint32_t bar, uint32_t bytes) {
                  : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); ++it) {
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits until the mbarrier phase of `parity` completes, for at most limit_ns
+// of wall time (the GPU's global nanosecond timer); false when it gave up.
+// Each try_wait may suspend the thread for a while, so the limit is taken
+// from the clock, not from a count of tries (a count of 2^30 tries stays as
+// a backstop should the timer not advance).
+constexpr uint64_t kWaitNs = 1000000000ull;     // 1 s: every wait of a normal launch
+constexpr uint64_t kTestWaitNs = 10000000ull;   // 10 ms: the first wait under the wait test
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          uint64_t limit_ns = kWaitNs) {
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 0; it < (1u << 30); ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -117,6 +133,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
             : "r"(bar), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((it & 15u) == 15u && global_ns() - t0 > limit_ns) return false;
     }
     return false;
 }
@@ -201,16 +218,23 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         sb[kLsHidden + e] = L.params[kLsB2 + e];
     }
     if (t < kLsVec) sb[2 * kLsHidden + t] = L.params[kLsB3 + t];
+    // wait test (mdg_learned_wait_test): the first transaction is withheld,
+    // so the copy barrier's first phase never completes and the first wait
+    // runs out after kTestWaitNs; no copy and no MMA is in flight then
+    const bool wait_test = L.tc_wait_test != 0;
     if (t == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         // the weight images and the first tile's features, one transaction
         const int tile0 = blockIdx.x;
-        expect_tx(tbar, kWtcBytes + (tile0 < n_tiles ? kXBytes : 0));
-        bulk_load(smem_u32(sm), L.wb + kLsWb, kWtcBytes, tbar);
-        if (tile0 < n_tiles)
-            bulk_load(smem_u32(sm + kOffX), X + (size_t)tile0 * kLsTile * kLsFeat, kXBytes, tbar);
+        if (!wait_test) {
+            expect_tx(tbar, kWtcBytes + (tile0 < n_tiles ? kXBytes : 0));
+            bulk_load(smem_u32(sm), L.wb + kLsWb, kWtcBytes, tbar);
+            if (tile0 < n_tiles)
+                bulk_load(smem_u32(sm + kOffX), X + (size_t)tile0 * kLsTile * kLsFeat, kXBytes,
+                          tbar);
+        }
     }
     if (w == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -231,10 +255,15 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     constexpr uint32_t kLbo128 = kLsTile * 16, kLbo16 = kLsVec * 16, kSbo = 128;
     constexpr uint32_t id128 = idesc_bf16(128, 128), id16 = idesc_bf16(128, 16);
     uint32_t phase = 0, tphase = 0;
-    bool ok = true, copy_pending = true;  // the weights (and first tile) are on their way
+    // copies and MMAs this CTA has started and not yet seen complete: what a
+    // CTA that gives up must wait for before it frees the tensor memory
+    bool ok = true, copy_pending = !wait_test, mma_pending = false;
+    bool first_wait = true;
     for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         const int row = tile * kLsTile + t;
-        ok = mbar_wait(tbar, tphase);  // this tile's features (and the weights) landed
+        // this tile's features (and, the first time, the weights) landed
+        ok = mbar_wait(tbar, tphase, (first_wait && wait_test) ? kTestWaitNs : kWaitNs);
+        first_wait = false;
         ok = __syncthreads_and(ok);
         if (!ok) break;
         tphase ^= 1;
@@ -247,9 +276,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                          sdesc(a_w1 + ks * 2 * kLbo128, kLbo128, kSbo), id128, ks);
             mma_commit(bar);
         }
+        mma_pending = true;
         ok = mbar_wait(bar, phase);
         ok = __syncthreads_and(ok);
         if (!ok) break;
+        mma_pending = false;
         phase ^= 1;
         fence_after();
         const int next = tile + gridDim.x;
@@ -270,9 +301,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                          sdesc(a_w2 + ks * 2 * kLbo128, kLbo128, kSbo), id128, ks);
             mma_commit(bar);
         }
+        mma_pending = true;
         ok = mbar_wait(bar, phase);
         ok = __syncthreads_and(ok);
         if (!ok) break;
+        mma_pending = false;
         phase ^= 1;
         fence_after();
         epilogue_hidden(tm + lane_base + kLsHidden, sb + kLsHidden, Hs, t);
@@ -287,9 +320,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                          sdesc(a_w3 + ks * 2 * kLbo16, kLbo16, kSbo), id16, ks);
             mma_commit(bar);
         }
+        mma_pending = true;
         ok = mbar_wait(bar, phase);
         ok = __syncthreads_and(ok);
         if (!ok) break;
+        mma_pending = false;
         phase ^= 1;
         fence_after();
         float o[16];
@@ -316,12 +351,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         fence_before();  // accumulator reads before the next tile's MMAs
     }
     if (t == 0) {
-        if (!ok) {
-            // a wait gave up: report, then let the MMAs and copies in flight
-            // finish (bounded) before the tensor memory is freed
-            raise_status(status, MDG_ERR_TIMEOUT);
-            mbar_wait(bar, phase);
-        }
+        // a wait gave up: report, then let the MMAs and copies still in
+        // flight finish (waits with the full limit) before the tensor memory
+        // is freed and the CTA's shared memory released
+        if (!ok) raise_status(status, MDG_ERR_TIMEOUT);
+        if (mma_pending) mbar_wait(bar, phase);
         if (copy_pending) mbar_wait(tbar, tphase);
     }
     fence_before();
@@ -372,6 +406,7 @@ cudaError_t ls_mlp_tc(mdg_system *s, int slot) {
     }
     const int grid = std::min(L.n_tiles, 2 * std::max(1, s->n_sms));
     k_ls_mlp_tc<<<grid, kTcThreads, kTcSmemAlloc, st>>>(L, L.n_rows, slot, s->status);
+    L.tc_wait_test = 0;  // one launch only
     s->launches += 1;
     return cudaGetLastError();
 }

@@ -120,7 +120,7 @@ struct SpArgs {
     const SysDev *__restrict__ sys;
     const int *__restrict__ atom_sys;
     int n_excl, n_14, n_pad;
-    float rc2, rs2, sw_inv_den, beta, ewald_fc;
+    float rc, rc2, rs2, sw_inv_den, beta, ewald_fc;
     int do_excl, do_lj14, do_coul14;
     float excl_weight;  // weight of the excluded-pair reciprocal correction's force
     unsigned long long *f;
@@ -163,14 +163,16 @@ __global__ void k_special(SpArgs a) {
                 e_rec = -qq * ef / r;
                 fr = a.excl_weight * qq * (a.ewald_fc * expf(-br * br) * r - ef) / (r2 * r);
             }
-        } else if (r2 <= a.rc2) {
-            if (DUMP) {
+        } else if (DUMP) {
+            // pair dump: the reference's own float32 pair test decides
+            if (ref_within32(a.x, i, j, sd, a.rc)) {
                 unsigned long long slot = atomicAdd(a.dump_count, 1ull);
                 if ((long long)slot < a.dump_cap) {
                     a.dump[2 * slot] = min(i, j);
                     a.dump[2 * slot + 1] = max(i, j);
                 }
             }
+        } else if (r2 <= a.rc2) {
             if (a.do_lj14) {
                 const float4 pi = a.lj[i], pj = a.lj[j];
                 const float sig = pi.z + pj.z;
@@ -254,6 +256,8 @@ NbArgs make_args(mdg_system *s) {
     a.dump_cap = s->dump_cap;
     a.dump_count = s->dump_count;
     a.perm = s->perm;
+    a.x = s->x;
+    a.rc_ref = s->cutoff;
     a.split = s->nb_split;
     a.persistent = s->nb_persistent > 0;
     a.n_items = s->n_clusters * s->nb_split;
@@ -271,6 +275,14 @@ cudaError_t launch_nonbonded(mdg_system *s, unsigned mask, int energy, int dump)
     if (!want_lj && !want_c) return cudaSuccess;
     NbArgs a = make_args(s);
     a.lj_on = want_lj ? 1 : 0;
+    if (dump) {
+        // the pair dump searches a little beyond the cutoff and lets the
+        // reference's float32 test (ref_within32) decide each candidate:
+        // the packed float32 coordinates differ from the reference's by
+        // rounding (~1e-5 A), far below this margin
+        a.rc = s->cutoff + kDumpMargin;
+        a.rc2 = a.rc * a.rc;
+    }
     const bool sw = s->rswitch > 0 && s->rswitch < s->cutoff;
     cudaError_t err = cudaSuccess;
     const int coul_tile = (want_c && s->coul_mode == MDG_COUL_EWALD) ? MDG_COUL_EWALD : MDG_COUL_NONE;
@@ -302,6 +314,7 @@ cudaError_t launch_special(mdg_system *s, unsigned mask, int energy, int dump) {
     a.n_pad = s->n_pad;
     a.sys = s->sys_dev;
     a.atom_sys = s->atom_sys;
+    a.rc = s->cutoff;
     a.rc2 = s->cutoff * s->cutoff;
     const double rs = s->rswitch > 0 ? s->rswitch : s->cutoff;
     a.rs2 = (float)(rs * rs);

@@ -40,6 +40,8 @@ struct NbArgs {
     long long dump_cap;
     unsigned long long *dump_count;
     const int *perm;
+    const double *x;  // FP64 state, atom order (pair dump: the reference's pair test)
+    float rc_ref;     // pair dump: the cutoff of that test (the search uses rc + a margin)
     int split;        // work items (one warp each) per i-cluster
     int persistent;   // 1: warps pull items from `queue` until none is left
     int n_items;      // n_clusters * split
@@ -51,6 +53,8 @@ namespace {
 
 constexpr int kRing = 64;
 constexpr unsigned kFull = 0xffffffffu;
+// the pair dump's search radius beyond the cutoff (A)
+constexpr float kDumpMargin = 0.01f;
 
 // Abramowitz & Stegun 7.1.26: erfc(x) ~ t(a1 + t(a2 + t(a3 + t(a4 + t a5)))) e^{-x^2},
 // t = 1/(1 + p x), |error| <= 1.5e-7
@@ -138,11 +142,15 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
             // atom with itself); every use below selects them away
             const bool inc = (r2 <= a.rc2) && !(mk & lanebit);
             if (DUMP && inc) {
-                unsigned long long slot = atomicAdd(a.dump_count, 1ull);
-                if ((long long)slot < a.dump_cap) {
-                    int pj_atom = a.perm[__float_as_int(aux.w)], pi_atom = a.perm[ik];
-                    a.dump[2 * slot] = min(pi_atom, pj_atom);
-                    a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
+                // a candidate of the widened search; the reference's own
+                // float32 test decides
+                const int pj_atom = a.perm[__float_as_int(aux.w)], pi_atom = a.perm[ik];
+                if (ref_within32(a.x, pi_atom, pj_atom, sd, a.rc_ref)) {
+                    unsigned long long slot = atomicAdd(a.dump_count, 1ull);
+                    if ((long long)slot < a.dump_cap) {
+                        a.dump[2 * slot] = min(pi_atom, pj_atom);
+                        a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
+                    }
                 }
             }
             const float rinv = rsqrtf(r2);

@@ -603,7 +603,10 @@ cudaError_t launch_pme(mdg_system *s, int energy, int *cufft_status) {
                                                   g.sys_ids, s->energy);
         s->launches += 1;
     }
+    // weight 0 (an impulse inner step that only reports the energy): the
+    // potential grid is never gathered, so the backward transform is skipped
     for (PmeGroup &g : p.groups) {
+        if (a.weight == 0.f) break;
         cufftResult r = cufftSetStream(g.plan_b, st);
         if (r == CUFFT_SUCCESS)
             r = cufftExecC2R(g.plan_b, (cufftComplex *)(p.grid_c + g.cgrid_off), p.grid_r + g.grid_off);

@@ -44,7 +44,10 @@ __global__ void k_bin(double *__restrict__ x, int n, const SysDev *__restrict__ 
     for (int k = 0; k < 3; ++k) {
         const double L = d.Ld[k];
         double p = x[3 * i + k];
-        ok = ok && isfinite(p);
+        // particle loss as mdpy's wrap_positions defines it (mdpy/utils/pbc.py:
+        // 30-34): a non-finite coordinate, or one two or more box lengths
+        // from the central image (|round(x / L)| >= 2)
+        ok = ok && isfinite(p) && fabs(rint(p * d.invLd[k])) < 2.0;
         p -= L * floor(p / L);
         if (p >= L) p -= L;
         if (!(p >= 0.0)) p = 0.0;

@@ -95,6 +95,47 @@ static inline int is_listed(const int *row, int width, int j) {
 }
 
 /*
+ * The reference's pair test in its own float32 arithmetic: d = x_j - x_i,
+ * scaled by the float32 inverse box, minus its rounded value, scaled back
+ * (unwrap_vec, mdpy/utils/pbc.py:38-43), r = sqrt of the left-to-right sum
+ * of squares (np.linalg.norm, charmm_nonbonded_constraint.py:85-90), r <= rc.
+ * Every operation rounds once (the library is built with -ffp-contract=off,
+ * so no multiply-add is fused on any host).
+ */
+static inline int ref_within32(const float *pos, int i, int j, const float *pbc_diag,
+                               float cutoff) {
+    float d[3];
+    for (int k = 0; k < 3; ++k) {
+        float L = pbc_diag[k];
+        float s = (pos[3 * j + k] - pos[3 * i + k]) * (1.0f / L);
+        s = s - rintf(s);
+        d[k] = s * L;
+    }
+    float r = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    return r <= cutoff;
+}
+
+/* all unordered pairs i<j (not excluded) that pass ref_within32: the set the
+ * reference's kernel would visit if its cell walk missed no periodic
+ * neighbour; all pairs, O(n^2) */
+long ORC_API orc_pairs_bruteforce_ref32(const float *pos, int n, const float *pbc_diag,
+                                        float cutoff, const int *excl, int excl_width,
+                                        int *pairs_out, long cap) {
+    long np = 0;
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            if (excl_width > 0 && is_listed(excl + (long)i * excl_width, excl_width, j)) continue;
+            if (!ref_within32(pos, i, j, pbc_diag, cutoff)) continue;
+            if (np < cap) {
+                pairs_out[2 * np] = i;
+                pairs_out[2 * np + 1] = j;
+            }
+            ++np;
+        }
+    return np;
+}
+
+/*
  * Pairs the reference's nonbonded kernel visits with r <= rc
  * (charmm_nonbonded_constraint.py:75-90): j lies in one of the 27 cells
  * (c_i + t) mod n (the kernel subtracts n for indices >= n and relies on
@@ -137,15 +178,7 @@ long ORC_API orc_ref_pairs(const float *pos, int n, const float *pbc_diag, float
                         if (j <= i) continue;
                         if (excl_width > 0 && is_listed(excl + (long)i * excl_width, excl_width, j))
                             continue;
-                        float d[3];
-                        for (int k = 0; k < 3; ++k) {
-                            float L = pbc_diag[k];
-                            float s = (pos[3 * j + k] - pos[3 * i + k]) * (1.0f / L);
-                            s = s - rintf(s);
-                            d[k] = s * L;
-                        }
-                        float r = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-                        if (r <= cutoff) {
+                        if (ref_within32(pos, i, j, pbc_diag, cutoff)) {
                             if (np < cap) {
                                 pairs_out[2 * np] = i;
                                 pairs_out[2 * np + 1] = j;
@@ -286,11 +319,33 @@ long ORC_API orc_pairs_bruteforce(const double *pos, int n, const double *box, d
  * visit: thread-safe and order-deterministic under a static schedule.
  * energies[0] = LJ, energies[1] = Coulomb.
  */
+/*
+ * orc_nonbonded_rows: the same loop for the atoms rows[0..nrows) only (forces
+ * (nrows, 3) on those atoms; energies count only the pairs visited from
+ * them).  rows == NULL means every atom in order.
+ */
+void ORC_API orc_nonbonded_rows(const double *pos, int n, const double *box,
+                                const double *params, const double *q, const int *excl,
+                                int excl_width, const int *scal, int scal_width, double rc,
+                                double rs, int use_switch, int lj_on, int coul_mode, double beta,
+                                double kcoul, const int *rows, int nrows, double *forces,
+                                double *energies);
+
 void ORC_API orc_nonbonded(const double *pos, int n, const double *box, const double *params,
                            const double *q, const int *excl, int excl_width, const int *scal,
                            int scal_width, double rc, double rs, int use_switch, int lj_on,
                            int coul_mode, double beta, double kcoul, double *forces,
                            double *energies) {
+    orc_nonbonded_rows(pos, n, box, params, q, excl, excl_width, scal, scal_width, rc, rs,
+                       use_switch, lj_on, coul_mode, beta, kcoul, NULL, n, forces, energies);
+}
+
+void ORC_API orc_nonbonded_rows(const double *pos, int n, const double *box,
+                                const double *params, const double *q, const int *excl,
+                                int excl_width, const int *scal, int scal_width, double rc,
+                                double rs, int use_switch, int lj_on, int coul_mode, double beta,
+                                double kcoul, const int *rows, int nrows, double *forces,
+                                double *energies) {
     cellgrid g;
     double search = (coul_mode == 2) ? 1e300 : rc;
     if (coul_mode == 2) {
@@ -307,7 +362,8 @@ void ORC_API orc_nonbonded(const double *pos, int n, const double *box, const do
     const double two_over_sqrtpi = 1.1283791670955126;
     double e_lj = 0, e_c = 0;
 #pragma omp parallel for schedule(static) reduction(+ : e_lj, e_c)
-    for (int i = 0; i < n; ++i) {
+    for (int r = 0; r < nrows; ++r) {
+        const int i = rows ? rows[r] : r;
         double fi[3] = {0, 0, 0};
         const int *xrow = excl_width > 0 ? excl + (long)i * excl_width : NULL;
         const int *srow = scal_width > 0 ? scal + (long)i * scal_width : NULL;
@@ -350,7 +406,7 @@ void ORC_API orc_nonbonded(const double *pos, int n, const double *box, const do
                 for (int k = 0; k < 3; ++k) fi[k] -= fr * d[k];
             }
         });
-        for (int k = 0; k < 3; ++k) forces[3 * i + k] = fi[k];
+        for (int k = 0; k < 3; ++k) forces[3 * (size_t)r + k] = fi[k];
     }
     energies[0] = e_lj;
     energies[1] = e_c;

@@ -50,7 +50,10 @@ def build(force=False):
         return _LIB_PATH
     os.makedirs(_BUILD, exist_ok=True)
     tmp = _LIB_PATH + ".%d.tmp" % os.getpid()
-    base = ["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-o", tmp, src, "-lm"]
+    # -ffp-contract=off: the float32 restatements round every operation as
+    # the reference does, on x86 and on Arm (where gcc would fuse a*b+c)
+    base = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11", "-o", tmp, src,
+            "-lm"]
     try:
         subprocess.run(base[:1] + ["-fopenmp"] + base[1:], check=True, capture_output=True)
     except subprocess.CalledProcessError:
@@ -65,6 +68,9 @@ def lib():
         if _lib is None:
             build()
             L = ctypes.CDLL(_LIB_PATH)
+            L.orc_pairs_bruteforce_ref32.restype = ctypes.c_long
+            L.orc_pairs_bruteforce_ref32.argtypes = [_fp, ctypes.c_int, _fp, ctypes.c_float, _ip,
+                                                     ctypes.c_int, _ip, ctypes.c_long]
             L.orc_ref_pairs.restype = ctypes.c_long
             L.orc_ref_pairs.argtypes = [_fp, ctypes.c_int, _fp, ctypes.c_float, _ip, _ip, _ip,
                                         ctypes.c_int, _ip, ctypes.c_long]
@@ -138,6 +144,23 @@ def ref_pairs(positions_f32, pbc_diag, cutoff, cell_index, num_cell_vec, exclusi
         cap = int(got)
 
 
+def pairs_bruteforce_ref32(positions_f32, pbc_diag, cutoff, exclusions):
+    """All unordered non-excluded pairs (i<j) that pass the reference's own
+    float32 pair test (mdg_oracle.c:ref_within32), over all pairs."""
+    pos, pp = _f(positions_f32)
+    diag, dp_ = _f(pbc_diag)
+    ex, exp_ = _i(exclusions)
+    width = ex.shape[1] if ex.ndim == 2 else 0
+    cap = 1 << 16
+    while True:
+        out = np.zeros((cap, 2), dtype=np.int32)
+        got = lib().orc_pairs_bruteforce_ref32(pp, pos.shape[0], dp_, cutoff, exp_, width,
+                                               out.ctypes.data_as(_ip), cap)
+        if got <= cap:
+            return out[:got]
+        cap = int(got)
+
+
 def pairs_bruteforce(positions, box, cutoff):
     """All unordered minimum-image pairs with r <= cutoff (FP64)."""
     pos, pp = _d(positions)
@@ -177,9 +200,11 @@ def pair_set_digest(pairs, n):
 # nonbonded, Ewald, PME
 # --------------------------------------------------------------------------
 def nonbonded(positions, box, params, charges, exclusions, scaling, cutoff, *,
-              switch=None, lj=True, coulomb="none", beta=0.0, kcoul=None):
+              switch=None, lj=True, coulomb="none", beta=0.0, kcoul=None, rows=None):
     """FP64 LJ / Coulomb forces and energies; ``coulomb`` in
-    {'none', 'ewald', 'bare'} (see mdg_oracle.c:orc_nonbonded)."""
+    {'none', 'ewald', 'bare'} (see mdg_oracle.c:orc_nonbonded).  With ``rows``
+    (atom indices) only those atoms' forces are computed and returned, in
+    that order (orc_nonbonded_rows); energies then count only their pairs."""
     from mdpy_gb300 import unit as U
 
     kc = U.COULOMB_K if kcoul is None else kcoul
@@ -190,13 +215,21 @@ def nonbonded(positions, box, params, charges, exclusions, scaling, cutoff, *,
     q, qp = _d(np.asarray(charges, dtype=np.float64).reshape(n))
     ex, exp_ = _i(np.asarray(exclusions).reshape(n, -1))
     sc, scp = _i(np.asarray(scaling).reshape(n, -1))
-    f = np.zeros((n, 3))
     e = np.zeros(2)
     mode = {"none": 0, "ewald": 1, "bare": 2}[coulomb]
-    lib().orc_nonbonded(pp, n, bp, prp, qp, exp_, ex.shape[1], scp, sc.shape[1],
-                        ctypes.c_double(cutoff), ctypes.c_double(switch or 0.0),
-                        int(switch is not None), int(bool(lj)), mode, ctypes.c_double(beta),
-                        ctypes.c_double(kc), f.ctypes.data_as(_dp), e.ctypes.data_as(_dp))
+    args = (pp, n, bp, prp, qp, exp_, ex.shape[1], scp, sc.shape[1], ctypes.c_double(cutoff),
+            ctypes.c_double(switch or 0.0), int(switch is not None), int(bool(lj)), mode,
+            ctypes.c_double(beta), ctypes.c_double(kc))
+    if rows is None:
+        f = np.zeros((n, 3))
+        lib().orc_nonbonded(*args, f.ctypes.data_as(_dp), e.ctypes.data_as(_dp))
+    else:
+        rw, rwp = _i(np.asarray(rows).reshape(-1))
+        if rw.size and (rw.min() < 0 or rw.max() >= n):
+            raise IndexError("rows outside 0..%d" % (n - 1))
+        f = np.zeros((rw.size, 3))
+        lib().orc_nonbonded_rows(*args, rwp, rw.size, f.ctypes.data_as(_dp),
+                                 e.ctypes.data_as(_dp))
     return f, {"lj": e[0], "coulomb": e[1]}
 
 

@@ -82,3 +82,23 @@ def rel_rms_excluding(a, b, drop):
     keep = np.ones(len(a), dtype=bool)
     keep[np.asarray(drop, dtype=np.int64)] = False
     return rel_rms(np.asarray(a)[keep], np.asarray(b)[keep])
+
+
+def ref32_pairs(orc, positions, box, rc, exclusions=None):
+    """The pair set the reference's own float32 pair test gives over all
+    pairs (oracle ref_within32), from positions as mdg_get_positions reports
+    them (wrapped into [-L/2, L/2) as mdpy wraps) rounded to float32."""
+    pos32 = np.asarray(positions, dtype=np.float64).astype(np.float32)
+    n = pos32.shape[0]
+    diag = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)).astype(np.float32)
+    ex = np.full((n, 1), -1, dtype=np.int32) if exclusions is None else exclusions
+    return pairs_to_set(orc.pairs_bruteforce_ref32(pos32, diag, float(rc), ex).reshape(-1, 2))
+
+
+def cutoff_band(orc, positions, box, rc, width=1e-4):
+    """Pairs whose FP64 minimum-image distance lies within ``width`` A of rc:
+    where float32 rounding decides which side a pair falls."""
+    pos = np.asarray(positions, dtype=np.float64)
+    outer = pairs_to_set(orc.pairs_bruteforce(pos, box, rc + width).reshape(-1, 2))
+    inner = pairs_to_set(orc.pairs_bruteforce(pos, box, rc - width).reshape(-1, 2))
+    return outer - inner

@@ -235,6 +235,23 @@ def test_step_host_continuation_keeps_forces(lib):
     a.check_status()
     b.step_host_ptr(xm.ctypes.data, vm.ctypes.data, 1, mask, xb.ctypes.data, vb.ctypes.data, eb)
     assert np.array_equal(a.get_positions(), xb) and np.array_equal(a.get_velocities(), vb)
+    # moved positions without velocities: the speculative step on the old
+    # state is undone (velocities and step counter put back) and redone
+    xm2 = np.ascontiguousarray(xb - 2e-3)
+    a.set_positions(xm2)
+    a.integrate(1, mask, want_energy=True)
+    keb = b.step_host_ptr(xm2.ctypes.data, 0, 1, mask, xb.ctypes.data, vb.ctypes.data, eb)
+    ea, kea = a.get_energies()
+    assert np.array_equal(a.get_positions(), xb) and np.array_equal(a.get_velocities(), vb)
+    assert np.array_equal(ea, eb) and kea == keb
+    assert a.step == b.step
+    # and the trajectories carry on together (same Philox step numbers)
+    for step in range(3):
+        a.integrate(1, mask, want_energy=True)
+        b.step_host_ptr(xb.ctypes.data, vb.ctypes.data, 1, mask, xb.ctypes.data,
+                        vb.ctypes.data, eb)
+        assert np.array_equal(a.get_positions(), xb), step
+        assert np.array_equal(a.get_velocities(), vb), step
 
 
 def test_mts_impulse_equations(lib):
@@ -308,3 +325,38 @@ def test_mts_energy_reported_at_inner_steps(lib):
         ep, _ = probe.system.get_energies()
         assert abs(e[lib.TERM_COUL_RECIP] - ep[lib.TERM_COUL_RECIP]) < 1e-6 * abs(ep[lib.TERM_COUL_RECIP]) + 1e-6
         probe.system.close()
+
+
+@pytest.mark.parametrize("bad", ["nan", "far"])
+def test_particle_loss_raised_by_the_device(lib, bad):
+    """A non-finite position, or one several boxes from the central image
+    (mdpy's ParticleLossError rule, mdpy/utils/pbc.py:30-34), set from the
+    host through the C ABI: the device re-sort of the next step flags it and
+    the status read raises ParticleLossError.  The system stays usable: good
+    positions afterwards step normally."""
+    from mdpy_gb300 import systems
+    from mdpy_gb300.error import ParticleLossError
+
+    w = systems.water_box(300, 21.0, seed=2)
+    ens = _ensemble(w, rc=9.0, K=24)
+    s = ens.system
+    s.integrator_config(lib.INTEGRATOR_LANGEVIN, 1.0, 300.0, 0.001, 3)
+    s.integrate(3, ens.term_mask, want_energy=False)
+    s.check_status()
+    x = s.get_positions()
+    v = s.get_velocities()
+    x_bad = x.copy()
+    if bad == "nan":
+        x_bad[17, 1] = np.nan
+    else:
+        x_bad[17, 0] += 3.0 * w.box[0]
+    s.set_positions(x_bad)
+    s.integrate(2, ens.term_mask, want_energy=False)
+    with pytest.raises(ParticleLossError):
+        s.check_status()
+    s.set_positions(x)
+    s.set_velocities(v)
+    s.integrate(2, ens.term_mask, want_energy=True)
+    s.check_status()
+    e, ke = s.get_energies()
+    assert np.all(np.isfinite(e)) and np.isfinite(ke)

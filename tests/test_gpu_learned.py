@@ -350,3 +350,35 @@ def test_field_gradient_term_vs_finite_differences(lib):
     err, ref = np.array(err), np.array(ref)
     # (B-spline second derivatives of an order-4 PME grid of ~0.94 A spacing)
     assert np.sqrt(np.mean(err ** 2)) < 0.15 * np.sqrt(np.mean(ref ** 2))
+
+
+def test_tensor_core_wait_timeout_reports_and_recovers(lib):
+    """The tcgen05 kernel's mbarrier waits are bounded by wall time.  The
+    one-shot wait test withholds the kernel's first bulk copy, so its first
+    wait runs out (10 ms): the call reports DeviceTimeoutError (no MMA or copy
+    is in flight, the tensor memory is freed), and the next call works and
+    gives the same prediction as before."""
+    from mdpy_gb300 import systems
+    from mdpy_gb300.error import DeviceTimeoutError
+
+    w = systems.water_box(900, 30.0, seed=10)
+    ens = _ensemble(w)
+    s = ens.system
+    s.learned_config(RF, 1.0, 256)
+    s.learned_set_params(_params(6))
+    s.learned_frame(0)
+    s.learned_set_kernel(True)
+    g0 = s.learned_predict(0)
+    s.learned_wait_test()
+    with pytest.raises(DeviceTimeoutError):
+        s.learned_predict(0)
+    g1 = s.learned_predict(0)
+    assert np.array_equal(g0, g1)
+    # and once more, after a second timed-out launch in a row
+    s.learned_wait_test()
+    with pytest.raises(DeviceTimeoutError):
+        s.learned_predict(0)
+    assert np.array_equal(s.learned_predict(0), g0)
+    s.learned_set_kernel(False)
+    with pytest.raises(Exception):
+        s.learned_wait_test()   # only the tensor-core kernel has the test

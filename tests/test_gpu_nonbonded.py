@@ -4,11 +4,10 @@ oracle, and the pair set against the reference's cell-list enumeration."""
 import numpy as np
 import pytest
 
-from tests.helpers import REF_E_TOL, half_box_tie_atoms, rel_rms_excluding, make_system, min_image_r, pairs_to_set, rel_rms, water_lj_rows
+from tests.helpers import (REF_E_TOL, cutoff_band, half_box_tie_atoms, make_system, pairs_to_set,
+                           ref32_pairs, rel_rms, rel_rms_excluding, water_lj_rows)
 
 pytestmark = pytest.mark.gpu
-
-EPS_BAND = 1e-4  # A: pairs this close to the cutoff may fall either side in FP32
 
 
 def test_lj_four_atoms_matches_reference(lib, golden):
@@ -44,18 +43,11 @@ def test_lj_water_box_matches_reference(lib, golden):
     assert e[lib.TERM_LJ] == pytest.approx(float(golden["w900_e_lj"]), rel=REF_E_TOL)
 
 
-def _split_band(pairset, pos, box, rc):
-    lst = sorted(pairset)
-    if not lst:
-        return set(), set()
-    r = min_image_r(pos, box, lst)
-    far = {p for p, rr in zip(lst, r) if abs(rr - rc) > EPS_BAND}
-    return far, set(lst) - far
-
-
 def test_pair_set_matches_reference_cell_list(lib, golden, orc):
-    """3^3 reference cells: the GPU pair set equals the set the reference's
-    kernel visits (mdpy/constraint/charmm_nonbonded_constraint.py:75-90)."""
+    """3^3 reference cells: the GPU pair set equals, bit for bit, the set the
+    reference's kernel visits (mdpy/constraint/charmm_nonbonded_constraint.py:
+    75-90).  The dump decides r <= rc with the reference's own float32
+    arithmetic, so pairs at the cutoff fall on the reference's side."""
     pos32 = golden["w900_positions"]
     n = pos32.shape[0]
     ref = orc.ref_pairs(pos32, np.full(3, 30.0, np.float32), 12.0, golden["w900_cell_index"],
@@ -68,16 +60,20 @@ def test_pair_set_matches_reference_cell_list(lib, golden, orc):
                     positions=pos32.astype(np.float64))
     gpu = pairs_to_set(s.pairset())
     refs = pairs_to_set(ref)
-    diff = gpu ^ refs
-    far, band = _split_band(diff, pos32, 30.0, 12.0)
-    assert not far, "pairs differ away from the cutoff: %s" % sorted(far)[:10]
-    assert len(band) <= 4
+    # the pairs within 1e-4 A of the cutoff, where FP32 rounding decides
+    band = cutoff_band(orc, pos32, 30.0, 12.0)
+    band = {p for p in band if golden["w900_bonded"][p[0]].tolist().count(p[1]) == 0}
+    print("cutoff band: %d pairs within 1e-4 A of rc, %d of them in the reference's set"
+          % (len(band), len(band & refs)))
+    assert gpu == refs, (sorted(gpu - refs)[:5], sorted(refs - gpu)[:5])
 
 
 def test_pair_set_4_cells_superset_of_reference(lib, golden, orc):
     """4^3 reference cells: the reference drops pairs across the periodic
-    wrap (its cell adjacency misses them); the GPU set equals brute force and
-    contains the reference's set."""
+    wrap (its cell adjacency misses them).  The GPU set equals, bit for bit,
+    the reference's float32 pair test over all pairs; it contains the
+    reference's set, and every pair it adds lies in cells the reference's
+    walk does not treat as neighbours."""
     pos32 = golden["sp50_positions"]
     n = pos32.shape[0]
     excl = np.full((n, 1), -1)
@@ -90,19 +86,20 @@ def test_pair_set_4_cells_superset_of_reference(lib, golden, orc):
                     charges=np.zeros(n), bonded=excl, cutoff=12.0,
                     positions=pos32.astype(np.float64))
     gpu = pairs_to_set(s.pairset())
-    far, _ = _split_band(gpu ^ bf, pos32, 50.0, 12.0)
-    assert not far
-    missing_in_ref = gpu - ref
-    far_ref, _ = _split_band(ref - gpu, pos32, 50.0, 12.0)
-    assert not far_ref
-    assert len(missing_in_ref) >= int(golden["sp50_bf_count"]) - int(golden["sp50_ref_count"]) - 2
-    # each pair the reference drops sits in cells that are not adjacent mod n
+    assert gpu == ref32_pairs(orc, pos32, 50.0, 12.0)
+    assert ref <= gpu
+    # each pair the reference drops sits in cells that are not adjacent mod n,
+    # and every GPU pair in adjacent cells is one the reference visits
     ci = golden["sp50_cell_index"]
     ncv = golden["sp50_num_cell_vec"]
-    for i, j in missing_in_ref:
+    missing_in_ref = gpu - ref
+    assert len(missing_in_ref) > 0
+    for i, j in gpu:
         d = np.abs(ci[i] - ci[j])
         d = np.minimum(d, ncv - d)
-        assert np.any(d > 1)
+        assert np.any(d > 1) == ((i, j) in missing_in_ref)
+    print("4^3 cells: %d pairs, %d dropped by the reference's cell walk"
+          % (len(gpu), len(missing_in_ref)))
 
 
 def test_lj_forces_four_cell_box_match_reference(lib, golden, orc):
@@ -251,10 +248,8 @@ def test_empty_and_tiny_systems(lib):
     s = make_system(lib, 33, 20.0, charges=np.zeros(33), lj=np.tile([1e-4, 3.0, 1e-4, 3.0], (33, 1)),
                     bonded=np.full((33, 1), -1), cutoff=9.0, positions=x)
     from oracle import oracle as O
-    bf = pairs_to_set(O.pairs_bruteforce(x, 20.0, 9.0))
     gpu = pairs_to_set(s.pairset())
-    far, _ = _split_band(gpu ^ bf, x, 20.0, 9.0)
-    assert not far
+    assert gpu == ref32_pairs(O, s.get_positions(), 20.0, 9.0)
 
 
 def test_cutoff_validation(lib):

@@ -37,6 +37,29 @@ def test_reference_pair_enumeration_digest(golden, orc):
     assert dig == int(golden["w900_pairs_digest"])
 
 
+def test_reference_float32_pair_test_over_all_pairs(golden, orc):
+    """At 3^3 cells the reference's cell walk visits every pair, so its own
+    float32 pair test applied to all pairs (the rule the GPU pair dump
+    follows) gives exactly the reference's set: same count, degrees and
+    digest as the golden vectors of the unmodified reference.  At 4^3 cells
+    the all-pairs set contains the reference's set (which drops wrap pairs)."""
+    from tests.helpers import ref32_pairs
+
+    pos = golden["w900_positions"]
+    n = pos.shape[0]
+    allp = orc.pairs_bruteforce_ref32(pos, np.full(3, 30.0, np.float32), 12.0,
+                                      golden["w900_bonded"])
+    cnt, deg, dig = orc.pair_set_digest(allp, n)
+    assert cnt == int(golden["w900_pairs_count"])
+    assert dig == int(golden["w900_pairs_digest"])
+    assert np.array_equal(deg, golden["w900_pairs_degree"])
+    pos50 = golden["sp50_positions"]
+    ref = pairs_to_set(orc.ref_pairs(pos50, np.full(3, 50.0, np.float32), 12.0,
+                                     golden["sp50_cell_index"], golden["sp50_num_cell_vec"],
+                                     np.full((pos50.shape[0], 1), -1)))
+    assert ref < ref32_pairs(orc, pos50, 50.0, 12.0)
+
+
 def test_lj_oracle_matches_reference_on_its_pair_set(golden, orc):
     """The FP64 LJ over the reference's pair set reproduces mdpy's float32
     CharmmNonbondedConstraint forces and energy (900 waters, 3^3 cells, where
