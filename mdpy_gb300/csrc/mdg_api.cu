@@ -1411,7 +1411,9 @@ MDG_API int mdg_step_host(mdg_system *s, const double *x_in, const double *v_in,
             CK(cudaMemcpyAsync(s->v, s->vsave, sizeof(double) * 3 * s->n,
                                cudaMemcpyDeviceToDevice, s->stream),
                "restore velocities");
-        s->step = step0;
+        // the step counter lives on the device too (the captured steps
+        // advance it there): both go back
+        if ((rc = mdg_set_step(s, step0))) return rc;
         s->steps_since_reorder = since0;
         s->forces_valid = 0;  // the redo takes the incoming positions as new
         return mdg_step_host(s, x_in, v_in, n_steps, mask, x_out, v_out, energies, kinetic);

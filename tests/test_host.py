@@ -396,3 +396,29 @@ def test_learned_training_loop_host_logic():
     temps = [c[1][2] for c in s.calls if c[0] == "integrator_config" and c[1][0] == _lib.INTEGRATOR_LANGEVIN]
     assert len(temps) >= 1 + 3 and all(280.0 <= t <= 320.0 for t in temps)
     assert names.count("learned_frame") == 2 * 8
+
+
+def test_reference_binding_imports_the_installed_reference():
+    """The reference-side binding's host part: the installed reference
+    (baseline/_ref) imports through the stubs, the binding subclasses its
+    Constraint, and its Topology of a water box carries the exclusions the
+    libmdg constraint hands to the device."""
+    from tests import ref_binding as RB
+
+    if not RB.reference_available():
+        pytest.skip("the reference is not installed in baseline/_ref")
+    from mdpy_gb300 import systems
+
+    w = systems.water_box(10, 10.0, seed=0)
+    t = RB.reference_topology(w)
+    t.join()   # what the reference's Ensemble does on construction
+    assert t.num_particles == 30
+    cls = RB.binding_class()
+    from mdpy.constraint import Constraint
+
+    assert issubclass(cls, Constraint)
+    # 1-2 and 1-3 partners of each atom of a water: the other two atoms
+    for i in range(30):
+        partners = sorted(int(p) for p in t.bonded_particles[i] if p >= 0)
+        m = i // 3
+        assert partners == [j for j in range(3 * m, 3 * m + 3) if j != i]
