@@ -204,8 +204,9 @@ MDG_API int mdg_step_host(mdg_system *sys, const double *x_in, const double *v_i
  *                              the block's grid patch, bit 1: gathering from one
  *                              (default 0);
  *   [MDG_SHAPE_HALF]           1: each half warp sweeps its own j list against 16
- *                              i atoms (j atoms within rc of those 16 only), 0:
- *                              one list against all 32 (default 0).
+ *                              i atoms (j atoms within rc of those 16 only); 2:
+ *                              each quarter warp against 8 i atoms; 0: one list
+ *                              against all 32 (default 0).
  * Results depend on the shape only through float rounding of partial sums
  * (the PME grid and tiling change nothing: int64 sums); for a fixed shape
  * they are bit-reproducible. */
@@ -223,7 +224,7 @@ MDG_API int mdg_get_launch_shape(mdg_system *sys, int *shape);
  * steps as mdg_integrate runs them (captured single-step graphs replayed from
  * a saved state, which is restored afterwards), else force evaluations of
  * `mask`.  Phase one varies the pair kernel (split 2/4/8 x persistent 0/20/24
- * x split rings 0/1 x half 0/1), phase two PME and the streams (block 64/128/256 x tiles
+ * x split rings 0/1 x half 0/1/2), phase two PME and the streams (block 64/128/256 x tiles
  * 0-3 x side priority 0/1) around phase one's best; then the four fastest and
  * the shape in use are re-timed, interleaved, over 4 x reps and the fastest
  * is kept; *best_ms (may be NULL) receives its time.  Leaves no valid force

@@ -528,6 +528,7 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     dfree(s->xq);
     dfree(s->bbox);
     dfree(s->hbox);
+    dfree(s->qbox);
     dfree(s->energy);
     dfree(s->status);
     dfree(s->stats);
@@ -1103,7 +1104,7 @@ static int apply_shape(mdg_system *s, const int *sh) {
         return fail(MDG_ERR_INVALID, "split_rings must be 0 or 1");
     if (pme_tiles < 0 || pme_tiles > 3)
         return fail(MDG_ERR_INVALID, "pme_tiles %d not in 0..3", pme_tiles);
-    if (half != 0 && half != 1) return fail(MDG_ERR_INVALID, "half must be 0 or 1");
+    if (half < 0 || half > 2) return fail(MDG_ERR_INVALID, "half must be 0, 1 or 2");
     s->nb_split = split;
     s->nb_persistent = persistent;
     s->nb_persistent_ctas = persistent * s->n_sms;
@@ -1153,7 +1154,8 @@ MDG_API int mdg_get_launch_shape(mdg_system *s, int *shape) {
 // so host launch gaps do not count), and puts the state back afterwards;
 // otherwise it times force evaluations of `mask`.  Phase one varies the pair
 // kernel (work items per cluster 2/4/8 x one CTA per item or 20/24 resident
-// CTAs per SM x split rings x half-warp i groups) with the PME fields of the shape in use; phase
+// CTAs per SM x split rings x i groups of 32 / 16 / 8 atoms) with the PME fields of the shape
+// in use; phase
 // two varies PME and the streams (block 64/128/256 x tiles 0-3 x side
 // priority) with phase one's best pair kernel; phase three re-times the four
 // fastest and the shape in use, interleaved, 4 x reps each, and keeps the
@@ -1226,7 +1228,7 @@ MDG_API int mdg_autotune(mdg_system *s, unsigned mask, int reps, double *best_ms
     for (int sp : {2, 4, 8})
         for (int pe : {0, 20, 24})
             for (int sr = 0; sr <= 1; ++sr)
-                for (int hf = 0; hf <= 1 && !rc && ce == cudaSuccess; ++hf) {
+                for (int hf = 0; hf <= 2 && !rc && ce == cudaSuccess; ++hf) {
                     Shape c = current;
                     c.sh[MDG_SHAPE_SPLIT] = sp;
                     c.sh[MDG_SHAPE_PERSISTENT] = pe;

@@ -139,6 +139,7 @@ struct PackArgs {
     float4 *xq;
     float4 *bbox;
     float4 *hbox;   // boxes of the two 16-slot halves: centre, half extents (x2)
+    float4 *qbox;   // boxes of the four 8-slot quarters: centre, half extents (x4)
     unsigned long long *f;
     const SysDev *sys;
     const int *cl_sys, *cl_col, *col_xy;
@@ -244,7 +245,8 @@ __device__ __forceinline__ void pack_cluster(const PackArgs &a, int warp, int k,
     float hix = valid ? p.x : -INFINITY, hiy = valid ? p.y : -INFINITY,
           hiz = valid ? p.z : -INFINITY;
     const unsigned vb = __ballot_sync(0xffffffffu, valid);
-    // the two 16-slot halves first, then the whole cluster
+    // the four 8-slot quarters first, then the two 16-slot halves, then the
+    // whole cluster
 #pragma unroll
     for (int o = 1; o <= 16; o <<= 1) {
         lox = fminf(lox, __shfl_xor_sync(0xffffffffu, lox, o));
@@ -253,6 +255,16 @@ __device__ __forceinline__ void pack_cluster(const PackArgs &a, int warp, int k,
         hix = fmaxf(hix, __shfl_xor_sync(0xffffffffu, hix, o));
         hiy = fmaxf(hiy, __shfl_xor_sync(0xffffffffu, hiy, o));
         hiz = fmaxf(hiz, __shfl_xor_sync(0xffffffffu, hiz, o));
+        if (o == 4 && (lane & 7) == 0) {
+            const int qg = lane >> 3;
+            const bool any = (vb >> (8 * qg)) & 0xffu;
+            a.qbox[8 * warp + 2 * qg] =
+                any ? make_float4(0.5f * (lox + hix), 0.5f * (loy + hiy), 0.5f * (loz + hiz), 1.0f)
+                    : make_float4(kFarAway, kFarAway, kFarAway, 0.0f);
+            a.qbox[8 * warp + 2 * qg + 1] =
+                any ? make_float4(0.5f * (hix - lox), 0.5f * (hiy - loy), 0.5f * (hiz - loz), 0.0f)
+                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
         if (o == 8 && (lane & 15) == 0) {
             const int h = lane >> 4;
             const bool any = (vb >> (16 * h)) & 0xffffu;
@@ -447,6 +459,7 @@ struct mdg_system {
     float4 *xq = nullptr;
     float4 *bbox = nullptr;
     float4 *hbox = nullptr;            // float4[4][clusters]: boxes of the 16-slot halves
+    float4 *qbox = nullptr;            // float4[8][clusters]: boxes of the 8-slot quarters
     long long *energy = nullptr;       // kEnergySlots per system
     int *status = nullptr;
     unsigned long long *stats = nullptr;  // 4 counters

@@ -39,6 +39,8 @@ namespace mdg {
 
 cudaError_t launch_nb_half(mdg_system *s, const NbArgs &a, int coul_tile, bool want_lj, bool sw,
                            int energy, int dump);  // mdg_nonbonded_half.cu
+cudaError_t launch_nb_quarter(mdg_system *s, const NbArgs &a, int coul_tile, bool want_lj,
+                              bool sw, int energy, int dump);  // mdg_nonbonded_quarter.cu
 
 namespace {
 
@@ -232,6 +234,7 @@ NbArgs make_args(mdg_system *s) {
     a.cl_sys = s->cl_sys;
     a.cl_col = s->cl_col;
     a.hbox = s->hbox;
+    a.qbox = s->qbox;
     a.col_xy = s->col_xy;
     a.col_rank = s->cell_rank;
     a.col_cl_start = s->col_cl_start;
@@ -287,8 +290,9 @@ cudaError_t launch_nonbonded(mdg_system *s, unsigned mask, int energy, int dump)
     cudaError_t err = cudaSuccess;
     const int coul_tile = (want_c && s->coul_mode == MDG_COUL_EWALD) ? MDG_COUL_EWALD : MDG_COUL_NONE;
     if (want_lj || coul_tile == MDG_COUL_EWALD) {
-        err = s->nb_half ? launch_nb_half(s, a, coul_tile, want_lj, sw, energy, dump)
-                         : dispatch_shape<false>(s, a, coul_tile, want_lj, sw, energy, dump);
+        err = s->nb_half == 2   ? launch_nb_quarter(s, a, coul_tile, want_lj, sw, energy, dump)
+              : s->nb_half == 1 ? launch_nb_half(s, a, coul_tile, want_lj, sw, energy, dump)
+                                : dispatch_shape<false>(s, a, coul_tile, want_lj, sw, energy, dump);
         s->launches += 1;
         if (err != cudaSuccess) return err;
     }

@@ -19,6 +19,7 @@ struct NbArgs {
     const SysDev *__restrict__ sys;
     const int *__restrict__ cl_sys;
     const float4 *__restrict__ hbox;       // boxes of each cluster's two 16-slot halves
+    const float4 *__restrict__ qbox;       // boxes of each cluster's four 8-slot quarters
     const int *__restrict__ cl_col;        // cluster -> global sort column
     const int *__restrict__ col_xy;        // global column -> (cx << 16) | cy
     const int *__restrict__ col_rank;      // system column (cx * ncy + cy) -> rank
@@ -85,6 +86,266 @@ __device__ __forceinline__ void lds128(unsigned addr, float4 &v) {
                  : "r"(addr));
 }
 
+// One pair: this lane's i atom (xi: position and scaled charge; pi: sigma/2
+// and sqrt(4 eps); ik its cluster-order slot) with one ring entry (xj:
+// shifted position and scaled charge; aux: the entry's sigma/2, sqrt(4 eps),
+// exclusion mask of the 32 i lanes and slot).  The force goes to the i
+// accumulators (fi) and to the entry's j accumulator (fj), the energies to
+// c_lj / c_c (FP32 within a chunk); WL: the entry carries LJ parameters.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool WL>
+__device__ __forceinline__ void pair_interact(const NbArgs &a, const SysDev &sd, const float4 &xi,
+                                              const float2 &pi, int ik, unsigned lanebit,
+                                              const float4 &xj, const float4 &aux, float &fix,
+                                              float &fiy, float &fiz, float &fjx, float &fjy,
+                                              float &fjz, float &c_lj, float &c_c,
+                                              unsigned long long &n_in) {
+    const unsigned mk = __float_as_uint(aux.z);
+    const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    // masked and out-of-range pairs may compute inf/NaN (r2 = 0 for an
+    // atom with itself); every use below selects them away
+    const bool inc = (r2 <= a.rc2) && !(mk & lanebit);
+    if (DUMP && inc) {
+        // a candidate of the widened search; the reference's own
+        // float32 test decides
+        const int pj_atom = a.perm[__float_as_int(aux.w)], pi_atom = a.perm[ik];
+        if (ref_within32(a.x, pi_atom, pj_atom, sd, a.rc_ref)) {
+            unsigned long long slot = atomicAdd(a.dump_count, 1ull);
+            if ((long long)slot < a.dump_cap) {
+                a.dump[2 * slot] = min(pi_atom, pj_atom);
+                a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
+            }
+        }
+    }
+    const float rinv = rsqrtf(r2);
+    const float rinv2 = rinv * rinv;
+    float fr = 0.f, elj = 0.f, ecl = 0.f;
+    if (LJ && WL) {
+        const float sig = pi.x + aux.x;
+        const float s2 = sig * sig * rinv2;
+        const float s6 = s2 * s2 * s2;
+        const float c6 = pi.y * aux.y * s6;
+        float flj = c6 * fmaf(12.0f, s6, -6.0f) * rinv2;
+        if (SWITCH) {
+            // CHARMM switch, branch free: below rs the clamped r^2 gives
+            // sw = 1 and dsw = 0 exactly
+            elj = c6 * (s6 - 1.0f);
+            const float r2c = fmaxf(r2, a.rs2);
+            const float u = a.rc2 - r2c;
+            const float sw = u * u * fmaf(2.0f, r2c, a.rc2 - 3.0f * a.rs2) * a.sw_inv_den;
+            const float dsw = 12.0f * u * (a.rs2 - r2c) * a.sw_inv_den;
+            flj = fmaf(flj, sw, -elj * dsw);
+            elj *= sw;
+        } else if (ENERGY) {
+            elj = c6 * (s6 - 1.0f);
+        }
+        fr = flj;
+    }
+    if (COUL == MDG_COUL_EWALD) {
+        const float qq = xi.w * xj.w;
+        const float r = r2 * rinv;
+        const float tt = __fdividef(1.0f, fmaf(a.beta_p, r, 1.0f));
+        const float poly =
+            tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, kAsA5, kAsA4), kAsA3), kAsA2), kAsA1);
+        const float ex = exp2f(-a.ewald_exp_c * r2);
+        const float ecf = qq * poly * ex * rinv;
+        fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecf), rinv2, fr);
+        // the force keeps the 1.5e-7 approximation in every variant (so a
+        // trajectory does not depend on when energies are reported); the
+        // reported energy uses the library erfc, whose error does not pile
+        // up over 10^6 pairs
+        if (ENERGY) ecl = qq * erfcf(a.beta * r) * rinv;
+    }
+    fr = inc ? fr : 0.f;
+    fix = fmaf(-fr, dx, fix);
+    fiy = fmaf(-fr, dy, fiy);
+    fiz = fmaf(-fr, dz, fiz);
+    fjx = fmaf(fr, dx, fjx);
+    fjy = fmaf(fr, dy, fjy);
+    fjz = fmaf(fr, dz, fjz);
+    if (ENERGY) {
+        c_lj += inc ? elj : 0.f;
+        c_c += inc ? ecl : 0.f;
+        n_in += __popc(__ballot_sync(kFull, inc));
+    }
+}
+
+// Candidate clusters of i-cluster I for work item `part` (of a.split): every
+// (J, periodic image) whose bounding box lies within rc of I's box, offered
+// to candidate(J, image code) in ballot order.  Work item `part` scans
+// batches part, part + split, ... of 32 clusters, so the split warps of one
+// i-cluster share its neighbourhood without talking to each other.
+// Balanced half shell: the cluster pair {I, J} (I != J) belongs to I when
+// I < J and I + J is odd, or when I > J and I + J is even -- every cluster
+// owns about half of its neighbours whatever its index; J == I is kept and
+// split by the lane mask.  Periodic images: the nearest image of J's box
+// centre, or all 27 when a box pair spans half the box.
+template <bool ENERGY, typename Cand>
+__device__ __forceinline__ void scan_candidates(const NbArgs &a, const int I, const int part,
+                                                const SysDev &sd, const float4 cI,
+                                                const float4 hI, Cand &&candidate,
+                                                unsigned &n_cand) {
+    const float L[3] = {sd.L[0], sd.L[1], sd.L[2]};
+    const float invL[3] = {sd.invL[0], sd.invL[1], sd.invL[2]};
+    const int cl_lo = sd.cl_off, cl_hi = sd.cl_off + sd.cl_cap;
+    const int sid = a.cl_sys[I];
+    const int lane = threadIdx.x & 31;
+    // every lane offers one (J, image) candidate; the hits go to candidate()
+    auto offer = [&](bool hit, int J, int code) {
+        unsigned b = __ballot_sync(kFull, hit);
+        if (ENERGY) n_cand += __popc(b);
+        while (b) {
+            const int src = __ffs(b) - 1;
+            b &= b - 1;
+            candidate(__shfl_sync(kFull, J, src), __shfl_sync(kFull, code, src));
+        }
+    };
+    // the half-shell owner rule
+    auto owned = [&](int J) { return J == I || ((I + J) & 1) == (I < J ? 1 : 0); };
+
+    // Column mode (systems whose columns span at least 2R+1 in x and y):
+    // candidates come only from the (2R+1)^2 columns around I's column, R =
+    // the column reach of rc plus twice the largest distance any cluster box
+    // has moved out of its column since the last re-sort.  Each column is a
+    // contiguous run of clusters; the runs are concatenated into one virtual
+    // list (warp scan of the run lengths) walked 32 at a time.
+    int R = 0;
+    bool colmode = sd.col_mode != 0;
+    if (colmode) {
+        const float ov = a.overhang[sid];
+        const float aw = fminf(L[0] / (float)sd.ncx, L[1] / (float)sd.ncy);
+        R = (int)floorf((a.rc + 2.f * ov) / aw) + 1;
+        colmode = 2 * R + 1 <= min(sd.ncx, sd.ncy);
+    }
+    if (colmode) {
+        const int pk = a.col_xy[a.cl_col[I]];
+        const int cx = pk >> 16, cy = pk & 0xffff;
+        const int side = 2 * R + 1, ncn = side * side;
+        const int base0 = a.col_cl_start[sd.col_off];
+        for (int cb = 0; cb < ncn; cb += 32) {
+            const int c = cb + lane;
+            int cnt = 0, start = 0, shc = 4;  // shc: (sx + 1) * 3 + (sy + 1)
+            if (c < ncn) {
+                int x2 = cx + c / side - R, y2 = cy + c % side - R;
+                const int sx = x2 < 0 ? -1 : (x2 >= sd.ncx ? 1 : 0);
+                const int sy = y2 < 0 ? -1 : (y2 >= sd.ncy ? 1 : 0);
+                x2 -= sx * sd.ncx;
+                y2 -= sy * sd.ncy;
+                const int gc = sd.col_off + a.col_rank[sd.col_off + x2 * sd.ncy + y2];
+                start = sd.cl_off + a.col_cl_start[gc] - base0;
+                cnt = a.col_ncl[gc];
+                shc = (sx + 1) * 3 + (sy + 1);
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(kFull, incl, 31);
+            for (int v0 = part * 32; v0 < total; v0 += a.split * 32) {
+                const int v = v0 + lane;
+                int lo = 0, hi = 31;  // first lane whose inclusive count exceeds v
+#pragma unroll
+                for (int it = 0; it < 5; ++it) {
+                    const int mid = (lo + hi) >> 1;
+                    const int im = __shfl_sync(kFull, incl, mid);
+                    if (im > v) hi = mid;
+                    else lo = mid + 1;
+                }
+                const int s_incl = __shfl_sync(kFull, incl, lo);
+                const int s_cnt = __shfl_sync(kFull, cnt, lo);
+                const int s_start = __shfl_sync(kFull, start, lo);
+                const int s_shc = __shfl_sync(kFull, shc, lo);
+                const int J = s_start + (v - (s_incl - s_cnt));
+                bool valid = v < total && owned(J);
+                float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                       hJ = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (valid) {
+                    cJ = a.bbox[2 * J];
+                    hJ = a.bbox[2 * J + 1];
+                }
+                valid = valid && cJ.w > 0.f;
+                // x and y images follow from the column wrap; z takes the
+                // nearest image of the box centres, or all three when a box
+                // pair spans half the box height
+                const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+                const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+                const float gx = fmaxf(fabsf(fmaf((float)(s_shc / 3 - 1), L[0], d[0])) - h[0], 0.f);
+                const float gy = fmaxf(fabsf(fmaf((float)(s_shc % 3 - 1), L[1], d[1])) - h[1], 0.f);
+                const float gxy = fmaf(gx, gx, gy * gy);
+                float nz = -rintf(d[2] * invL[2]);
+                nz = fminf(fmaxf(nz, -1.f), 1.f);
+                const float gz = fmaxf(fabsf(fmaf(nz, L[2], d[2])) - h[2], 0.f);
+                const bool near_hit = valid && fmaf(gz, gz, gxy) <= a.rc2;
+                const bool multi_z = valid && (h[2] + a.rc >= 0.5f * L[2]);
+                if (!__any_sync(kFull, multi_z)) {
+                    offer(near_hit, J, s_shc * 3 + (int)nz + 1);
+                } else {
+                    for (int zz = -1; zz <= 1; ++zz) {
+                        bool hit = near_hit && zz == (int)nz;
+                        if (multi_z) {
+                            const float g = fmaxf(fabsf(fmaf((float)zz, L[2], d[2])) - h[2], 0.f);
+                            hit = fmaf(g, g, gxy) <= a.rc2;
+                        }
+                        offer(hit, J, s_shc * 3 + zz + 1);
+                    }
+                }
+            }
+        }
+    } else {
+        // full scan of the system's clusters: work item `part` takes batches
+        // part, part + split, ... of 32 clusters
+        for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += a.split * 32) {
+            const int J = J0 + lane;
+            bool valid = J < cl_hi && owned(J);
+            float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
+                   hJ = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) {
+                cJ = a.bbox[2 * J];
+                hJ = a.bbox[2 * J + 1];
+            }
+            const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
+            const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
+            int ncode = 0;
+            float g2 = 0.f;
+            bool multi = false;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float nk = -rintf(d[k] * invL[k]);
+                nk = fminf(fmaxf(nk, -1.f), 1.f);
+                const float dd = fmaf(nk, L[k], d[k]);
+                const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                g2 = fmaf(gap, gap, g2);
+                ncode = ncode * 3 + (int)nk + 1;
+                multi = multi || (h[k] + a.rc >= 0.5f * L[k]);
+            }
+            valid = valid && cJ.w > 0.f;
+            multi = multi && valid;
+            const bool near_hit = valid && g2 <= a.rc2;
+            if (!__any_sync(kFull, multi)) {
+                offer(near_hit, J, ncode);
+            } else {
+                for (int code = 0; code < 27; ++code) {
+                    bool hit = near_hit && code == ncode;
+                    if (multi) {
+                        const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
+                        float gg = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            const float dd = fmaf((float)s3[k], L[k], d[k]);
+                            const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
+                            gg = fmaf(gap, gap, gg);
+                        }
+                        hit = gg <= a.rc2;
+                    }
+                    offer(hit, J, code);
+                }
+            }
+        }
+    }
+}
+
 // One work item: part `part` (of a.split) of i-cluster I's pair search.
 // HALF: the warp's two 16-lane halves sweep separate j lists, each holding
 // only the j atoms within rc of its own 16 i atoms' box.
@@ -97,12 +358,10 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
     float4 *const ringL2 = s_j + 4 * kRing, *const ringQ2 = s_j + 6 * kRing;
     const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
     if (cI.w == 0.f) return;  // all-padding cluster
-    // this cluster's system: its box, and the range of clusters it may pair with
+    // this cluster's system and its box
     const int sid = a.cl_sys[I];
     const SysDev &sd = a.sys[sid];
     const float L[3] = {sd.L[0], sd.L[1], sd.L[2]};
-    const float invL[3] = {sd.invL[0], sd.invL[1], sd.invL[2]};
-    const int cl_lo = sd.cl_off, cl_hi = sd.cl_off + sd.cl_cap;
     const int lane = threadIdx.x;
     const unsigned lt = (1u << lane) - 1u;
     const int ik = I * kCluster + lane;
@@ -135,75 +394,9 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         float fjx = 0.f, fjy = 0.f, fjz = 0.f;
         float c_lj = 0.f, c_c = 0.f;
         auto step = [&](const float4 &xj, const float4 &aux, unsigned shfl_mask) {
-            const unsigned mk = __float_as_uint(aux.z);
-            const float dx = xj.x - xi.x, dy = xj.y - xi.y, dz = xj.z - xi.z;
-            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            // masked and out-of-range pairs may compute inf/NaN (r2 = 0 for an
-            // atom with itself); every use below selects them away
-            const bool inc = (r2 <= a.rc2) && !(mk & lanebit);
-            if (DUMP && inc) {
-                // a candidate of the widened search; the reference's own
-                // float32 test decides
-                const int pj_atom = a.perm[__float_as_int(aux.w)], pi_atom = a.perm[ik];
-                if (ref_within32(a.x, pi_atom, pj_atom, sd, a.rc_ref)) {
-                    unsigned long long slot = atomicAdd(a.dump_count, 1ull);
-                    if ((long long)slot < a.dump_cap) {
-                        a.dump[2 * slot] = min(pi_atom, pj_atom);
-                        a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
-                    }
-                }
-            }
-            const float rinv = rsqrtf(r2);
-            const float rinv2 = rinv * rinv;
-            float fr = 0.f, elj = 0.f, ecl = 0.f;
-            if (LJ && WL) {
-                const float sig = pi.x + aux.x;
-                const float s2 = sig * sig * rinv2;
-                const float s6 = s2 * s2 * s2;
-                const float c6 = pi.y * aux.y * s6;
-                float flj = c6 * fmaf(12.0f, s6, -6.0f) * rinv2;
-                if (SWITCH) {
-                    // CHARMM switch, branch free: below rs the clamped r^2 gives
-                    // sw = 1 and dsw = 0 exactly
-                    elj = c6 * (s6 - 1.0f);
-                    const float r2c = fmaxf(r2, a.rs2);
-                    const float u = a.rc2 - r2c;
-                    const float sw = u * u * fmaf(2.0f, r2c, a.rc2 - 3.0f * a.rs2) * a.sw_inv_den;
-                    const float dsw = 12.0f * u * (a.rs2 - r2c) * a.sw_inv_den;
-                    flj = fmaf(flj, sw, -elj * dsw);
-                    elj *= sw;
-                } else if (ENERGY) {
-                    elj = c6 * (s6 - 1.0f);
-                }
-                fr = flj;
-            }
-            if (COUL == MDG_COUL_EWALD) {
-                const float qq = xi.w * xj.w;
-                const float r = r2 * rinv;
-                const float tt = __fdividef(1.0f, fmaf(a.beta_p, r, 1.0f));
-                const float poly =
-                    tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, kAsA5, kAsA4), kAsA3), kAsA2), kAsA1);
-                const float ex = exp2f(-a.ewald_exp_c * r2);
-                const float ecf = qq * poly * ex * rinv;
-                fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecf), rinv2, fr);
-                // the force keeps the 1.5e-7 approximation in every variant (so a
-                // trajectory does not depend on when energies are reported); the
-                // reported energy uses the library erfc, whose error does not pile
-                // up over 10^6 pairs
-                if (ENERGY) ecl = qq * erfcf(a.beta * r) * rinv;
-            }
-            fr = inc ? fr : 0.f;
-            fix = fmaf(-fr, dx, fix);
-            fiy = fmaf(-fr, dy, fiy);
-            fiz = fmaf(-fr, dz, fiz);
-            fjx = fmaf(fr, dx, fjx);
-            fjy = fmaf(fr, dy, fjy);
-            fjz = fmaf(fr, dz, fjz);
-            if (ENERGY) {
-                c_lj += inc ? elj : 0.f;
-                c_c += inc ? ecl : 0.f;
-                n_in += __popc(__ballot_sync(kFull, inc));
-            }
+            pair_interact<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, xi, pi, ik, lanebit, xj, aux,
+                                                             fix, fiy, fiz, fjx, fjy, fjz, c_lj,
+                                                             c_c, n_in);
             fjx = __shfl_xor_sync(kFull, fjx, shfl_mask);
             fjy = __shfl_xor_sync(kFull, fjy, shfl_mask);
             fjz = __shfl_xor_sync(kFull, fjz, shfl_mask);
@@ -370,169 +563,8 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         }
     };
 
-    // Candidate clusters.  Work item `part` scans batches part, part + split,
-    // ... of 32 clusters, so the split warps of one i-cluster share its
-    // neighbourhood without talking to each other.
-    // Balanced half shell: the cluster pair {I, J} (I != J) belongs to I when
-    // I < J and I + J is odd, or when I > J and I + J is even -- every cluster
-    // owns about half of its neighbours whatever its index; J == I is kept and
-    // split by the lane mask.  Periodic images: the nearest image of J's box
-    // centre, or all 27 when a box pair spans half the box.
     unsigned n_cand = 0;
-    // every lane offers one (J, image) candidate; the hits go to candidate()
-    auto offer = [&](bool hit, int J, int code) {
-        unsigned b = __ballot_sync(kFull, hit);
-        if (ENERGY) n_cand += __popc(b);
-        while (b) {
-            const int src = __ffs(b) - 1;
-            b &= b - 1;
-            candidate(__shfl_sync(kFull, J, src), __shfl_sync(kFull, code, src));
-        }
-    };
-    // the half-shell owner rule
-    auto owned = [&](int J) { return J == I || ((I + J) & 1) == (I < J ? 1 : 0); };
-
-    // Column mode (systems whose columns span at least 2R+1 in x and y):
-    // candidates come only from the (2R+1)^2 columns around I's column, R =
-    // the column reach of rc plus twice the largest distance any cluster box
-    // has moved out of its column since the last re-sort.  Each column is a
-    // contiguous run of clusters; the runs are concatenated into one virtual
-    // list (warp scan of the run lengths) walked 32 at a time.
-    int R = 0;
-    bool colmode = sd.col_mode != 0;
-    if (colmode) {
-        const float ov = a.overhang[sid];
-        const float aw = fminf(L[0] / (float)sd.ncx, L[1] / (float)sd.ncy);
-        R = (int)floorf((a.rc + 2.f * ov) / aw) + 1;
-        colmode = 2 * R + 1 <= min(sd.ncx, sd.ncy);
-    }
-    if (colmode) {
-        const int pk = a.col_xy[a.cl_col[I]];
-        const int cx = pk >> 16, cy = pk & 0xffff;
-        const int side = 2 * R + 1, ncn = side * side;
-        const int base0 = a.col_cl_start[sd.col_off];
-        for (int cb = 0; cb < ncn; cb += 32) {
-            const int c = cb + lane;
-            int cnt = 0, start = 0, shc = 4;  // shc: (sx + 1) * 3 + (sy + 1)
-            if (c < ncn) {
-                int x2 = cx + c / side - R, y2 = cy + c % side - R;
-                const int sx = x2 < 0 ? -1 : (x2 >= sd.ncx ? 1 : 0);
-                const int sy = y2 < 0 ? -1 : (y2 >= sd.ncy ? 1 : 0);
-                x2 -= sx * sd.ncx;
-                y2 -= sy * sd.ncy;
-                const int gc = sd.col_off + a.col_rank[sd.col_off + x2 * sd.ncy + y2];
-                start = sd.cl_off + a.col_cl_start[gc] - base0;
-                cnt = a.col_ncl[gc];
-                shc = (sx + 1) * 3 + (sy + 1);
-            }
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(kFull, incl, o);
-                if (lane >= o) incl += t;
-            }
-            const int total = __shfl_sync(kFull, incl, 31);
-            for (int v0 = part * 32; v0 < total; v0 += a.split * 32) {
-                const int v = v0 + lane;
-                int lo = 0, hi = 31;  // first lane whose inclusive count exceeds v
-#pragma unroll
-                for (int it = 0; it < 5; ++it) {
-                    const int mid = (lo + hi) >> 1;
-                    const int im = __shfl_sync(kFull, incl, mid);
-                    if (im > v) hi = mid;
-                    else lo = mid + 1;
-                }
-                const int s_incl = __shfl_sync(kFull, incl, lo);
-                const int s_cnt = __shfl_sync(kFull, cnt, lo);
-                const int s_start = __shfl_sync(kFull, start, lo);
-                const int s_shc = __shfl_sync(kFull, shc, lo);
-                const int J = s_start + (v - (s_incl - s_cnt));
-                bool valid = v < total && owned(J);
-                float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
-                       hJ = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (valid) {
-                    cJ = a.bbox[2 * J];
-                    hJ = a.bbox[2 * J + 1];
-                }
-                valid = valid && cJ.w > 0.f;
-                // x and y images follow from the column wrap; z takes the
-                // nearest image of the box centres, or all three when a box
-                // pair spans half the box height
-                const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
-                const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
-                const float gx = fmaxf(fabsf(fmaf((float)(s_shc / 3 - 1), L[0], d[0])) - h[0], 0.f);
-                const float gy = fmaxf(fabsf(fmaf((float)(s_shc % 3 - 1), L[1], d[1])) - h[1], 0.f);
-                const float gxy = fmaf(gx, gx, gy * gy);
-                float nz = -rintf(d[2] * invL[2]);
-                nz = fminf(fmaxf(nz, -1.f), 1.f);
-                const float gz = fmaxf(fabsf(fmaf(nz, L[2], d[2])) - h[2], 0.f);
-                const bool near_hit = valid && fmaf(gz, gz, gxy) <= a.rc2;
-                const bool multi_z = valid && (h[2] + a.rc >= 0.5f * L[2]);
-                if (!__any_sync(kFull, multi_z)) {
-                    offer(near_hit, J, s_shc * 3 + (int)nz + 1);
-                } else {
-                    for (int zz = -1; zz <= 1; ++zz) {
-                        bool hit = near_hit && zz == (int)nz;
-                        if (multi_z) {
-                            const float g = fmaxf(fabsf(fmaf((float)zz, L[2], d[2])) - h[2], 0.f);
-                            hit = fmaf(g, g, gxy) <= a.rc2;
-                        }
-                        offer(hit, J, s_shc * 3 + zz + 1);
-                    }
-                }
-            }
-        }
-    } else {
-        // full scan of the system's clusters: work item `part` takes batches
-        // part, part + split, ... of 32 clusters
-        for (int J0 = cl_lo + part * 32; J0 < cl_hi; J0 += a.split * 32) {
-            const int J = J0 + lane;
-            bool valid = J < cl_hi && owned(J);
-            float4 cJ = make_float4(kFarAway, kFarAway, kFarAway, 0.f),
-                   hJ = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (valid) {
-                cJ = a.bbox[2 * J];
-                hJ = a.bbox[2 * J + 1];
-            }
-            const float d[3] = {cJ.x - cI.x, cJ.y - cI.y, cJ.z - cI.z};
-            const float h[3] = {hI.x + hJ.x, hI.y + hJ.y, hI.z + hJ.z};
-            int ncode = 0;
-            float g2 = 0.f;
-            bool multi = false;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                float nk = -rintf(d[k] * invL[k]);
-                nk = fminf(fmaxf(nk, -1.f), 1.f);
-                const float dd = fmaf(nk, L[k], d[k]);
-                const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
-                g2 = fmaf(gap, gap, g2);
-                ncode = ncode * 3 + (int)nk + 1;
-                multi = multi || (h[k] + a.rc >= 0.5f * L[k]);
-            }
-            valid = valid && cJ.w > 0.f;
-            multi = multi && valid;
-            const bool near_hit = valid && g2 <= a.rc2;
-            if (!__any_sync(kFull, multi)) {
-                offer(near_hit, J, ncode);
-            } else {
-                for (int code = 0; code < 27; ++code) {
-                    bool hit = near_hit && code == ncode;
-                    if (multi) {
-                        const int s3[3] = {code / 9 - 1, (code / 3) % 3 - 1, code % 3 - 1};
-                        float gg = 0.f;
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) {
-                            const float dd = fmaf((float)s3[k], L[k], d[k]);
-                            const float gap = fmaxf(fabsf(dd) - h[k], 0.f);
-                            gg = fmaf(gap, gap, gg);
-                        }
-                        hit = gg <= a.rc2;
-                    }
-                    offer(hit, J, code);
-                }
-            }
-        }
-    }
+    scan_candidates<ENERGY>(a, I, part, sd, cI, hI, candidate, n_cand);
     // The partial last chunks, padded with far-away entries.  When both fit
     // in one chunk the charge-only entries join the LJ chunk (their LJ terms
     // are zero), so an item ends with at most one partial sweep.
@@ -608,6 +640,253 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
     }
 }
 
+// One work item of the quarter form: the warp's four 8-lane groups hold the
+// four 8-slot quarters of i-cluster I, and each group sweeps its own j lists
+// -- the j atoms within rc of its quarter's box, fewer than within rc of the
+// whole cluster's box.  Each group keeps two rings of 64 entries (LJ-
+// carrying and charge-only j atoms); a candidate cluster's atoms are tested
+// against the four quarter boxes (kept in shared memory) and appended to
+// the rings of the quarters they reach.  A sweep takes one 8-entry chunk
+// per group in 8 steps: lane (g, l) pairs its i atom with entry l ^ t of
+// its group's chunk, the j-force accumulators move by butterfly shuffles
+// inside the group, and after step 7 the lane owns entry l ^ 7's j force.
+// A group short of a chunk is padded with far-away entries only when
+// another group's ring nears capacity, and at the end of the item.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP>
+__device__ __forceinline__ void nb_item_q(const NbArgs &a, const int I, const int part,
+                                          float4 *s_j) {
+    constexpr int RQ = 64;  // entries per ring
+    // ring (group g, kind k: 0 = LJ, 1 = charge-only) at s_j + (2 g + k) 2 RQ;
+    // the four quarter boxes behind the eight rings
+    float4 *const qb = s_j + 16 * RQ;
+    const float4 cI = a.bbox[2 * I], hI = a.bbox[2 * I + 1];
+    if (cI.w == 0.f) return;  // all-padding cluster
+    const int sid = a.cl_sys[I];
+    const SysDev &sd = a.sys[sid];
+    const float L[3] = {sd.L[0], sd.L[1], sd.L[2]};
+    const int lane = threadIdx.x;
+    const int grp = lane >> 3, li = lane & 7;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned lanebit = 1u << lane;
+    const int ik = I * kCluster + lane;
+    const float4 xi = a.xq[ik];
+    const float2 pi = a.prm[ik];
+    const bool i_real = xi.x < 0.5f * kFarAway;
+    const int2 rI = a.prange[I];
+    const int ilo = I * kCluster;
+    __syncwarp();  // a previous item's reads of the boxes are done
+    if (lane < 8) qb[lane] = a.qbox[8 * I + lane];
+    __syncwarp();
+    auto ring = [&](int g, int k) { return s_j + (2 * g + k) * 2 * RQ; };
+    auto shared_addr = [](const float4 *p) { return (unsigned)__cvta_generic_to_shared(p); };
+
+    float fix = 0.f, fiy = 0.f, fiz = 0.f;
+    double acc_lj = 0.0, acc_c = 0.0;
+    unsigned long long n_eval = 0, n_in = 0;
+    // this lane's group's rings: first pending entry and pending count
+    int jbL = 0, jcL = 0, jbQ = 0, jcQ = 0;
+
+    auto push_j = [&](int jk, float fjx, float fjy, float fjz) {
+        if (jk >= 0 && !DUMP) {
+            if (!(fabsf(fjx) < kFixLimit && fabsf(fjy) < kFixLimit && fabsf(fjz) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            fix_red(&a.f[jk], to_fix(fjx));
+            fix_red(&a.f[a.n_pad + jk], to_fix(fjy));
+            fix_red(&a.f[2 * a.n_pad + jk], to_fix(fjz));
+        }
+    };
+    // a group short of a chunk of kind k gets far-away entries up to 8
+    auto pad = [&](int k, int jb, int jc) {
+        if (li >= jc)
+            put_entry(ring(grp, k), (jb + li) & (RQ - 1),
+                      make_float4(kFarAway, kFarAway, kFarAway, 0.f), make_float2(0.f, 0.f), kFull,
+                      -1);
+    };
+    // One 8-step sweep of one chunk per group (kind k of each group's ring),
+    // each step's entry loaded one step ahead; the chunk is 256-byte aligned,
+    // so entry l ^ t lives at (chunk | l << 5) ^ (t << 5).
+    auto sweep = [&](auto with_lj, int k, int jb) {
+        constexpr bool WL = decltype(with_lj)::value;
+        const unsigned sa = shared_addr(ring(grp, k) + 2 * jb) | ((unsigned)li << 5);
+        float fx = 0.f, fy = 0.f, fz = 0.f, c_lj = 0.f, c_c = 0.f;
+        float4 xa, aa, xb, ab;
+        lds128(sa, xa);
+        lds128(sa + 16u, aa);
+#pragma unroll 1
+        for (int t = 0; t < 8; t += 2) {
+            const unsigned o1 = sa ^ ((unsigned)(t + 1) << 5);
+            lds128(o1, xb);
+            lds128(o1 + 16u, ab);
+            pair_interact<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, xi, pi, ik, lanebit, xa, aa,
+                                                             fix, fiy, fiz, fx, fy, fz, c_lj, c_c,
+                                                             n_in);
+            fx = __shfl_xor_sync(kFull, fx, 1);
+            fy = __shfl_xor_sync(kFull, fy, 1);
+            fz = __shfl_xor_sync(kFull, fz, 1);
+            if (t < 6) {
+                const unsigned o2 = sa ^ ((unsigned)(t + 2) << 5);
+                lds128(o2, xa);
+                lds128(o2 + 16u, aa);
+            }
+            pair_interact<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, xi, pi, ik, lanebit, xb, ab,
+                                                             fix, fiy, fiz, fx, fy, fz, c_lj, c_c,
+                                                             n_in);
+            const int m = t < 6 ? ((t + 1) ^ (t + 2)) : 0;
+            fx = __shfl_xor_sync(kFull, fx, m);
+            fy = __shfl_xor_sync(kFull, fy, m);
+            fz = __shfl_xor_sync(kFull, fz, m);
+        }
+        float4 own;
+        lds128((sa ^ (7u << 5)) + 16u, own);
+        push_j(__float_as_int(own.w), fx, fy, fz);
+        if (ENERGY) {
+            acc_lj += (double)c_lj;
+            acc_c += (double)c_c;
+        }
+        n_eval += 256;
+        __syncwarp();
+    };
+    auto take = [](int &jb, int &jc) {
+        jb = (jb + 8) & (RQ - 1);
+        jc = max(jc - 8, 0);
+    };
+    // Sweeps after a candidate: a kind whose rings all hold a full chunk;
+    // then, while some group's ring could not take another candidate (more
+    // than 32 pending), padded sweeps of that kind.  At the end (final_)
+    // everything left is swept, padded.
+    auto drain = [&](bool final_) {
+        const int lim = final_ ? 0 : 32;
+        for (;;) {
+            if (__all_sync(kFull, jcL >= 8)) {
+                sweep(std::true_type{}, 0, jbL);
+                take(jbL, jcL);
+            } else if (__all_sync(kFull, jcQ >= 8)) {
+                sweep(std::false_type{}, 1, jbQ);
+                take(jbQ, jcQ);
+            } else if (__any_sync(kFull, jcQ > lim)) {
+                pad(1, jbQ, jcQ);
+                __syncwarp();
+                sweep(std::false_type{}, 1, jbQ);
+                take(jbQ, jcQ);
+            } else if (__any_sync(kFull, jcL > lim)) {
+                pad(0, jbL, jcL);
+                __syncwarp();
+                sweep(std::true_type{}, 0, jbL);
+                take(jbL, jcL);
+            } else {
+                break;
+            }
+        }
+    };
+
+    auto candidate = [&](int J, int code) {
+        float sx, sy, sz;
+        decode_shift(code, L, sx, sy, sz);
+        const int jk = J * kCluster + lane;
+        float4 xj = a.xq[jk];
+        xj.x += sx;
+        xj.y += sy;
+        xj.z += sz;
+        unsigned hm = 0u;  // the quarters this j atom reaches
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const float4 c = qb[2 * g], h = qb[2 * g + 1];
+            const float gx = fmaxf(fabsf(xj.x - c.x) - h.x, 0.f);
+            const float gy = fmaxf(fabsf(xj.y - c.y) - h.y, 0.f);
+            const float gz = fmaxf(fabsf(xj.z - c.z) - h.z, 0.f);
+            // a quarter with no atoms has a far-away box (w = 0), which
+            // far-away padding j slots would reach
+            if (c.w > 0.f && fmaf(gx, gx, fmaf(gy, gy, gz * gz)) <= a.rc2) hm |= 1u << g;
+        }
+        const float2 pj = hm ? a.prm[jk] : make_float2(0.f, 0.f);
+        const bool to_l = !a.split_rings || (LJ && pj.y != 0.f);
+        if (!to_l && !(COUL == MDG_COUL_EWALD || DUMP)) hm = 0u;
+        if (__ballot_sync(kFull, hm != 0u) == 0u) return;
+        unsigned m = 0u;  // exclusion mask of the 32 i lanes for this j atom
+        if (hm) {
+            if (J == I) m = kFull << lane;  // half shell inside the cluster
+            if (rI.y >= J * kCluster && rI.x < (J + 1) * kCluster) {
+                for (int w = 0; w < a.pw; ++w) {
+                    const int p = a.partners[(size_t)jk * a.pw + w];
+                    if (p >= 0) {
+                        const int pk = (p & 0x3fffffff) - ilo;
+                        if (pk >= 0 && pk < kCluster) m |= 1u << pk;
+                    }
+                }
+            }
+        }
+        const int endL = jbL + jcL, endQ = jbQ + jcQ;  // this lane's group's ring ends
+        int addL = 0, addQ = 0;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            const bool hit = (hm >> g) & 1u;
+            const unsigned bL = __ballot_sync(kFull, hit && to_l);
+            const unsigned bQ = __ballot_sync(kFull, hit && !to_l);
+            const int eL = __shfl_sync(kFull, endL, 8 * g), eQ = __shfl_sync(kFull, endQ, 8 * g);
+            if (hit) {
+                if (to_l) put_entry(ring(g, 0), (eL + __popc(bL & lt)) & (RQ - 1), xj, pj, m, jk);
+                else put_entry(ring(g, 1), (eQ + __popc(bQ & lt)) & (RQ - 1), xj, pj, m, jk);
+            }
+            if (g == grp) {
+                addL = __popc(bL);
+                addQ = __popc(bQ);
+            }
+        }
+        jcL += addL;
+        jcQ += addQ;
+        __syncwarp();
+        drain(false);
+    };
+
+    unsigned n_cand = 0;
+    scan_candidates<ENERGY>(a, I, part, sd, cI, hI, candidate, n_cand);
+    drain(true);
+
+    if (!DUMP && i_real) {
+        if (!(fabsf(fix) < kFixLimit && fabsf(fiy) < kFixLimit && fabsf(fiz) < kFixLimit))
+            raise_status(a.status, MDG_ERR_OVERFLOW);
+        fix_red(&a.f[ik], to_fix(fix));
+        fix_red(&a.f[a.n_pad + ik], to_fix(fiy));
+        fix_red(&a.f[2 * a.n_pad + ik], to_fix(fiz));
+    }
+    if (ENERGY) {
+        const double el = warp_sum_d(acc_lj), ee = warp_sum_d(acc_c);
+        if (lane == 0) {
+            if (!(fabs(el) < kFixLimit && fabs(ee) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            long long *es = a.energy + sid * kEnergySlots;
+            fix_red((unsigned long long *)&es[MDG_TERM_LJ], to_fix_d(el));
+            fix_red((unsigned long long *)&es[MDG_TERM_COUL_REAL], to_fix_d(ee));
+            atomicAdd(&a.stats[0], n_eval);
+            atomicAdd(&a.stats[1], n_in);
+            atomicAdd(&a.stats[2], (unsigned long long)n_cand);
+            if (part == 0) atomicAdd(&a.stats[3], 1ull);
+        }
+    }
+}
+
+// The quarter form as a kernel, in the grid form or the persistent form as
+// k_nonbonded below.  16 KB of rings per one-warp CTA: 13 CTAs per SM.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP>
+__global__ void __launch_bounds__(32, ENERGY ? 12 : 13) k_nonbonded_q(NbArgs a) {
+    // eight rings of 64 entries of 32 bytes, each 8-entry chunk on a
+    // 256-byte boundary, then the four quarter boxes
+    __shared__ __align__(1024) float4 s_j[16 * 64 + 8];
+    if (!a.persistent) {
+        nb_item_q<COUL, LJ, SWITCH, ENERGY, DUMP>(a, blockIdx.x / a.split, blockIdx.x % a.split,
+                                                  s_j);
+        return;
+    }
+    for (;;) {
+        int item = 0;
+        if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
+        item = __shfl_sync(kFull, item, 0);
+        if (item >= a.n_items) break;
+        __syncwarp();
+        nb_item_q<COUL, LJ, SWITCH, ENERGY, DUMP>(a, item / a.split, item % a.split, s_j);
+    }
+}
+
 // Grid form: one one-warp CTA per work item, scheduled by the hardware.
 // Persistent form: enough warps to fill the GPU once, each pulling work
 // items from a device counter until none is left.
@@ -636,9 +915,10 @@ cudaError_t dispatch_nb(mdg_system *s, const NbArgs &a, int energy, int dump) {
     dim3 grid(a.persistent ? s->nb_persistent_ctas : a.n_items), block(32);
     if (a.persistent && cudaMemsetAsync(a.queue, 0, sizeof(int), s->stream) != cudaSuccess)
         return cudaGetLastError();
-    if (dump)
-        k_nonbonded<COUL, LJ, SW, false, true, HALF><<<grid, block, 0, s->stream>>>(a);
-    else if (energy)
+    if (dump) {
+        if constexpr (COUL == MDG_COUL_EWALD && LJ && !SW)
+            k_nonbonded<COUL, LJ, SW, false, true, HALF><<<grid, block, 0, s->stream>>>(a);
+    } else if (energy)
         k_nonbonded<COUL, LJ, SW, true, false, HALF><<<grid, block, 0, s->stream>>>(a);
     else
         k_nonbonded<COUL, LJ, SW, false, false, HALF><<<grid, block, 0, s->stream>>>(a);
@@ -649,6 +929,9 @@ cudaError_t dispatch_nb(mdg_system *s, const NbArgs &a, int energy, int dump) {
 template <bool HALF>
 cudaError_t dispatch_shape(mdg_system *s, const NbArgs &a, int coul_tile, bool want_lj, bool sw,
                            int energy, int dump) {
+    // the pair-set dump decides pairs by the reference's test alone, whatever
+    // the terms: one instantiation serves every configuration
+    if (dump) return dispatch_nb<MDG_COUL_EWALD, true, false, HALF>(s, a, 0, 1);
     if (coul_tile == MDG_COUL_EWALD && !want_lj)
         return dispatch_nb<MDG_COUL_EWALD, false, false, HALF>(s, a, energy, dump);
     if (coul_tile == MDG_COUL_EWALD)

@@ -354,6 +354,7 @@ int prepare_sort_grid(mdg_system *s) {
             (rc = realloc_dev(&s->f, 3 * (size_t)n_pad)) ||
             (rc = realloc_dev(&s->bbox, 2 * (size_t)n_clusters)) ||
             (rc = realloc_dev(&s->hbox, 4 * (size_t)n_clusters)) ||
+            (rc = realloc_dev(&s->qbox, 8 * (size_t)n_clusters)) ||
             (rc = realloc_dev(&s->cluster_partner_range, n_clusters)) ||
             (rc = realloc_dev(&s->cl_sys, n_clusters)) ||
             (rc = realloc_dev(&s->cl_col, n_clusters)) ||
@@ -432,6 +433,7 @@ PackArgs make_pack_args(mdg_system *s) {
     a.xq = s->xq;
     a.bbox = s->bbox;
     a.hbox = s->hbox;
+    a.qbox = s->qbox;
     a.f = s->f;
     a.sys = s->sys_dev;
     a.cl_sys = s->cl_sys;

@@ -31,7 +31,7 @@ def test_every_shape_gives_the_same_forces(lib, orc, edge, n_waters):
     ref_pairs = None
     ref_f = None
     for split in (1, 2, 4, 8, 16):
-        for persistent, half in ((0, 0), (20, 0), (0, 1), (20, 1)):
+        for persistent, half in ((0, 0), (20, 0), (0, 1), (20, 1), (0, 2), (12, 2)):
             s.set_launch_shape(split, persistent, (64, 128, 256)[split % 3], split % 2,
                                (split // 2) % 2, split % 4, half)
             pairs = pairs_to_set(s.pairset())
@@ -67,7 +67,7 @@ def test_autotune_keeps_a_valid_shape(lib, orc):
     assert r["split"] in (2, 4, 8) and r["pme_block"] in (64, 128, 256)
     assert r["persistent"] in (0, 20, 24) and r["side_priority"] in (0, 1)
     assert r["split_rings"] in (0, 1) and r["pme_tiles"] in (0, 1, 2, 3) and r["tuned_ms"] > 0
-    assert r["half"] in (0, 1)
+    assert r["half"] in (0, 1, 2)
     with pytest.raises(Exception, match="no force evaluation"):
         s.get_forces()
     s.compute_forces(mask)

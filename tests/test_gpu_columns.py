@@ -26,7 +26,7 @@ def _box():
     return systems.water_box(5000, 53.0, seed=21)   # 15,000 atoms, 8 x 8 columns
 
 
-@pytest.mark.parametrize("half", [0, 1])
+@pytest.mark.parametrize("half", [0, 1, 2])
 @pytest.mark.parametrize("rc", [10.0, 14.0, 20.0])
 def test_column_pair_set_equals_bruteforce(lib, orc, rc, half):
     w = _box()
@@ -46,7 +46,7 @@ def test_column_pair_set_equals_bruteforce(lib, orc, rc, half):
     assert abs(s.nonbonded_stats()["pairs_in_cutoff"] - len(gpu)) <= len(band)
 
 
-@pytest.mark.parametrize("half", [0, 1])
+@pytest.mark.parametrize("half", [0, 1, 2])
 @pytest.mark.parametrize("n_waters,edge", [(5000, 53.0), (900, 30.0)])
 def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge, half):
     """400 Langevin steps at 900 K with no re-sort: unbonded H atoms fly
@@ -70,7 +70,7 @@ def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge, half):
     _same_pairs(orc, gpu, x, w.box, 12.0)
 
 
-@pytest.mark.parametrize("half", [0, 1])
+@pytest.mark.parametrize("half", [0, 1, 2])
 def test_column_forces_vs_oracle(lib, orc, half):
     w = _box()
     t = w.topology

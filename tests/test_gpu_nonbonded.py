@@ -66,6 +66,10 @@ def test_pair_set_matches_reference_cell_list(lib, golden, orc):
     print("cutoff band: %d pairs within 1e-4 A of rc, %d of them in the reference's set"
           % (len(band), len(band & refs)))
     assert gpu == refs, (sorted(gpu - refs)[:5], sorted(refs - gpu)[:5])
+    # every form of the pair kernel (i groups of 32, 16 and 8 atoms) finds it
+    for half in (1, 2):
+        s.set_launch_shape(half=half)
+        assert pairs_to_set(s.pairset()) == refs, half
 
 
 def test_pair_set_4_cells_superset_of_reference(lib, golden, orc):
