@@ -88,6 +88,10 @@ def parse():
                         "then 40 learned steps with PME every K steps; prints the times")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch shape instead of timing the alternatives")
+    p.add_argument("--shape", default="",
+                   help="launch-shape fields to pin instead of autotuning, e.g. 'half=2,split=4' "
+                        "(fields: split, persistent, pme_block, side_priority, split_rings, "
+                        "pme_tiles, half)")
     p.add_argument("--waters", type=int, default=None)
     p.add_argument("--box", type=float, default=None)
     p.add_argument("--beads", type=int, default=None)
@@ -111,6 +115,12 @@ def parse():
     a.box = b if a.box is None else a.box
     a.beads = beads if a.beads is None else a.beads
     a.grid = grid
+    a.shape_fields = {}
+    for kv in [t for t in a.shape.split(",") if t.strip()]:
+        k, v = kv.split("=")
+        a.shape_fields[k.strip()] = int(v)
+    if a.shape_fields:
+        a.no_autotune = True
     if a.nve_ps is None:
         a.nve_ps = 100.0 if a.workload == "water90k" else 0.0
     if a.workload == "water1m":
@@ -216,6 +226,8 @@ def run_batch(a, world, rank, local):
     mask = b.term_mask
     sysm.set_graph_mode(_lib.GRAPH_STEP)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    if a.shape_fields:
+        sysm.set_launch_shape(**dict(sysm.launch_shape, **a.shape_fields))
     shape = sysm.launch_shape if a.no_autotune else sysm.autotune(mask, reps=5)
     sysm.integrate(max(a.warmup, 3), mask, want_energy=False)
     torch.cuda.synchronize()
@@ -884,6 +896,8 @@ def main():
     mask = ens.term_mask
     sysm.set_graph_mode(_lib.GRAPH_STEP)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    if a.shape_fields:
+        sysm.set_launch_shape(**dict(sysm.launch_shape, **a.shape_fields))
     shape = sysm.launch_shape if a.no_autotune else sysm.autotune(mask, reps=10)
 
     # warm-up (graphs captured here)
@@ -925,6 +939,7 @@ def main():
     stats = sysm.nonbonded_stats()
     stage_ms = {}
     for name, stage in (("pack", _lib.STAGE_PACK), ("nonbonded", _lib.STAGE_NONBONDED),
+                        ("nonbonded_with_energies", _lib.STAGE_NONBONDED_ENERGY),
                         ("special", _lib.STAGE_SPECIAL), ("pme", _lib.STAGE_PME),
                         ("bonded", _lib.STAGE_BONDED), ("integrate", _lib.STAGE_INTEGRATE),
                         ("reorder", _lib.STAGE_REORDER)):
@@ -1144,7 +1159,7 @@ def end_to_end(sysm, mask, n, a, world, local):
         for k in range(steps):
             want = (k + 1) % energy_every == 0
             sysm.step_host_ptr(x_h.data_ptr(), v_h.data_ptr(), 1, mask, x_h.data_ptr(),
-                               v_h.data_ptr(), e_terms if want else None)
+                               v_h.data_ptr(), e_terms if want else None, want_kinetic=want)
 
     out = {}
     for name, every in (("energies_every_step", 1), ("energies_every_10_steps", 10)):

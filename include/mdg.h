@@ -379,6 +379,7 @@ MDG_API int mdg_set_graph_mode(mdg_system *sys, int mode);
 #define MDG_STAGE_BONDED 4
 #define MDG_STAGE_REORDER 5
 #define MDG_STAGE_INTEGRATE 6 /* pre + post update kernels */
+#define MDG_STAGE_NONBONDED_ENERGY 7 /* the pair kernel's variant that also sums energies */
 MDG_API int mdg_launch_stage(mdg_system *sys, int stage, unsigned mask);
 
 #ifdef __cplusplus

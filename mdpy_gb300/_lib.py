@@ -112,7 +112,7 @@ SIGNATURES = {
 
 GRAPH_CHUNK, GRAPH_STEP = 0, 1
 STAGE_PACK, STAGE_NONBONDED, STAGE_SPECIAL, STAGE_PME, STAGE_BONDED, STAGE_REORDER, \
-    STAGE_INTEGRATE = range(7)
+    STAGE_INTEGRATE, STAGE_NONBONDED_ENERGY = range(8)
 
 _lib = None
 

@@ -1899,6 +1899,9 @@ MDG_API int mdg_launch_stage(mdg_system *s, int stage, unsigned mask) {
     switch (stage) {
         case MDG_STAGE_PACK: CK(launch_pack(s), "pack"); break;
         case MDG_STAGE_NONBONDED: CK(launch_nonbonded(s, mask, 0, 0), "nonbonded"); break;
+        case MDG_STAGE_NONBONDED_ENERGY:
+            CK(launch_nonbonded(s, mask, 1, 0), "nonbonded with energies");
+            break;
         case MDG_STAGE_SPECIAL: CK(launch_special(s, mask, 0, 0), "special"); break;
         case MDG_STAGE_PME: {
             if (!s->pme.on) return fail(MDG_ERR_STATE, "PME is not configured");

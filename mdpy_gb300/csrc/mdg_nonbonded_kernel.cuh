@@ -80,6 +80,21 @@ __device__ __forceinline__ void put_entry(float4 *ring, int pos, float4 xq, floa
     ring[2 * pos + 1] = make_float4(prm.x, prm.y, __uint_as_float(mask), __int_as_float(jk));
 }
 
+// 2^x and 1/x as single special-function instructions (PTX ex2.approx /
+// rcp.approx, flush-to-zero; relative error below 2^-22): the pair kernel's
+// arguments stay in normal range (2^x with x in [-16, 0], 1/x with x in
+// [1, 2.1])
+__device__ __forceinline__ float fast_exp2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float fast_rcp(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 __device__ __forceinline__ void lds128(unsigned addr, float4 &v) {
     asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
                  : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
@@ -144,10 +159,10 @@ __device__ __forceinline__ void pair_interact(const NbArgs &a, const SysDev &sd,
     if (COUL == MDG_COUL_EWALD) {
         const float qq = xi.w * xj.w;
         const float r = r2 * rinv;
-        const float tt = __fdividef(1.0f, fmaf(a.beta_p, r, 1.0f));
+        const float tt = fast_rcp(fmaf(a.beta_p, r, 1.0f));
         const float poly =
             tt * fmaf(tt, fmaf(tt, fmaf(tt, fmaf(tt, kAsA5, kAsA4), kAsA3), kAsA2), kAsA1);
-        const float ex = exp2f(-a.ewald_exp_c * r2);
+        const float ex = fast_exp2(-a.ewald_exp_c * r2);
         const float ecf = qq * poly * ex * rinv;
         fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecf), rinv2, fr);
         // the force keeps the 1.5e-7 approximation in every variant (so a
