@@ -71,15 +71,6 @@ __device__ __forceinline__ void decode_shift(int code, const float (&L)[3], floa
     sz = (float)(code % 3 - 1) * L[2];
 }
 
-// One j entry staged in shared memory, two float4: the shifted coordinates
-// + charge, and (sigma/2, sqrt(4 eps), exclusion mask of the 32 i lanes,
-// cluster-order index) -- one 128-bit shared load each in the sweep.
-__device__ __forceinline__ void put_entry(float4 *ring, int pos, float4 xq, float2 prm,
-                                          unsigned mask, int jk) {
-    ring[2 * pos] = xq;
-    ring[2 * pos + 1] = make_float4(prm.x, prm.y, __uint_as_float(mask), __int_as_float(jk));
-}
-
 // 2^x and 1/x as single special-function instructions (PTX ex2.approx /
 // rcp.approx, flush-to-zero; relative error below 2^-22): the pair kernel's
 // arguments stay in normal range (2^x with x in [-16, 0], 1/x with x in
@@ -115,6 +106,32 @@ __device__ __forceinline__ float erfc_energy(float x) {
     // exp(u) = 2^(u log2 e)
     return t * fast_exp2(fmaf(-x, x, p) * 1.4426950408889634f);
 }
+
+// One j entry staged in shared memory, two float4: the shifted coordinates
+// + charge, and (sigma/2, sqrt(4 eps), exclusion mask of the 32 i lanes,
+// cluster-order index) -- one 128-bit shared load each in the sweep.  An
+// entry whose ring position has bit 2 set keeps its two halves swapped: a
+// quarter warp's eight lanes read eight consecutive entries 32 bytes apart,
+// and the swap puts their 16-byte halves on distinct banks (without it, two
+// lanes of every eight share banks).  Entry e of a chunk therefore has its
+// coordinates at byte (e << 5) ^ ((e & 4) << 2) and the rest 16 bytes away.
+__device__ __forceinline__ void put_entry(float4 *ring, int pos, float4 xq, float2 prm,
+                                          unsigned mask, int jk) {
+    const int sw = (pos >> 2) & 1;
+    ring[2 * pos + sw] = xq;
+    ring[2 * pos + (sw ^ 1)] =
+        make_float4(prm.x, prm.y, __uint_as_float(mask), __int_as_float(jk));
+}
+
+__device__ __forceinline__ void copy_entry(const float4 *src, int ps, float4 *dst, int pd) {
+    const int ss = (ps >> 2) & 1, sd = (pd >> 2) & 1;
+    const float4 x = src[2 * ps + ss], au = src[2 * ps + (ss ^ 1)];
+    dst[2 * pd + sd] = x;
+    dst[2 * pd + (sd ^ 1)] = au;
+}
+
+// byte offset of the coordinates half of entry e within its chunk
+__device__ __forceinline__ unsigned entry_off(unsigned e) { return (e << 5) ^ ((e & 4u) << 2); }
 
 __device__ __forceinline__ void lds128(unsigned addr, float4 &v) {
     asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
@@ -421,7 +438,7 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
     // the lane that pairs with e next (a butterfly shuffle with mask
     // t ^ (t + 1)).  After step 31 lane l owns entry l ^ 31's complete j
     // force.  The chunk is 1024-byte aligned, so entry l ^ t lives at
-    // (chunk | l << 5) ^ (t << 5): one logic op per step for the address.
+    // chunk | entry_off(l ^ t): one logic op per step for the address.
     const unsigned lanebit = 1u << lane;
     auto chunk = [&](auto with_lj, auto width, unsigned sa) {
         constexpr bool WL = decltype(with_lj)::value;
@@ -440,32 +457,34 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         // each step's entry is loaded one step ahead, so its shared-memory
         // latency overlaps the previous step's arithmetic
         float4 xa, aa, xb, ab;
-        lds128(sa | ((unsigned)li << 5), xa);
-        lds128((sa | ((unsigned)li << 5)) + 16u, aa);
+        const unsigned s0 = sa | entry_off((unsigned)li);
+        lds128(s0, xa);
+        lds128(s0 ^ 16u, aa);
 #pragma unroll 1
         for (int t0 = 0; t0 < W; t0 += 4) {
-            const unsigned sb = sa | ((unsigned)(li ^ t0) << 5);
+            // entries (l ^ t0) .. (l ^ t0) ^ 3 share bit 2, hence the swap
+            const unsigned sb = sa | entry_off((unsigned)(li ^ t0));
             // masks t ^ (t + 1) for t = t0 .. t0 + 3 (below W: a half warp's
             // accumulators stay in that half); none after the last step
             const unsigned m3 = t0 == W - 4 ? 0u : (unsigned)((t0 + 3) ^ (t0 + 4));
             lds128(sb ^ 32u, xb);
-            lds128((sb ^ 32u) + 16u, ab);
+            lds128(sb ^ 48u, ab);
             step(xa, aa, 1u);
             lds128(sb ^ 64u, xa);
-            lds128((sb ^ 64u) + 16u, aa);
+            lds128(sb ^ 80u, aa);
             step(xb, ab, 3u);
             lds128(sb ^ 96u, xb);
-            lds128((sb ^ 96u) + 16u, ab);
+            lds128(sb ^ 112u, ab);
             step(xa, aa, 1u);
             if (t0 < W - 4) {
-                const unsigned nb = sa | ((unsigned)(li ^ (t0 + 4)) << 5);
+                const unsigned nb = sa | entry_off((unsigned)(li ^ (t0 + 4)));
                 lds128(nb, xa);
-                lds128(nb + 16u, aa);
+                lds128(nb ^ 16u, aa);
             }
             step(xb, ab, m3);
         }
         float4 own;
-        lds128(sa + ((unsigned)(li ^ (W - 1)) << 5) + 16u, own);
+        lds128((sa | entry_off((unsigned)(li ^ (W - 1)))) ^ 16u, own);
         const int jk = __float_as_int(own.w);
         if (jk >= 0 && !DUMP) {
             if (!(fabsf(fjx) < kFixLimit && fabsf(fjy) < kFixLimit && fabsf(fjz) < kFixLimit))
@@ -608,14 +627,10 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         if ((jcQ > 0 || jcQ2 > 0) && jcL + jcQ <= 16 && jcL2 + jcQ2 <= 16) {
             const int h = lane >> 4, li = lane & 15;
             const int cq = h ? jcQ2 : jcQ;
-            if (li < cq) {
-                const float4 *src = (h ? ringQ2 : ringQ) + 2 * (((h ? jbQ2 : jbQ) + li) & (kRing - 1));
-                float4 *dst = (h ? ringL2 : ringL) +
-                              2 * (((h ? jbL2 : jbL) + (h ? jcL2 : jcL) + li) & (kRing - 1));
-                const float4 e0 = src[0], e1 = src[1];
-                dst[0] = e0;
-                dst[1] = e1;
-            }
+            if (li < cq)
+                copy_entry(h ? ringQ2 : ringQ, ((h ? jbQ2 : jbQ) + li) & (kRing - 1),
+                           h ? ringL2 : ringL,
+                           ((h ? jbL2 : jbL) + (h ? jcL2 : jcL) + li) & (kRing - 1));
             jcL += jcQ;
             jcQ = 0;
             jcL2 += jcQ2;
@@ -626,13 +641,8 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         while (jcQ > 0 || jcQ2 > 0) sweep16(std::false_type{});
     }
     if (!HALF && jcQ > 0 && jcL + jcQ <= 32) {
-        if (lane < jcQ) {
-            const float4 *src = ringQ + 2 * ((jbQ + lane) & (kRing - 1));
-            float4 *dst = ringL + 2 * ((jbL + jcL + lane) & (kRing - 1));
-            const float4 e0 = src[0], e1 = src[1];
-            dst[0] = e0;
-            dst[1] = e1;
-        }
+        if (lane < jcQ)
+            copy_entry(ringQ, (jbQ + lane) & (kRing - 1), ringL, (jbL + jcL + lane) & (kRing - 1));
         jcL += jcQ;
         jcQ = 0;
         __syncwarp();
@@ -740,19 +750,20 @@ __device__ __forceinline__ void nb_item_q(const NbArgs &a, const int I, const in
     };
     // One 8-step sweep of one chunk per group (kind k of each group's ring),
     // each step's entry loaded one step ahead; the chunk is 256-byte aligned,
-    // so entry l ^ t lives at (chunk | l << 5) ^ (t << 5).
+    // so entry l ^ t lives at chunk | entry_off(l ^ t).
     auto sweep = [&](auto with_lj, int k, int jb) {
         constexpr bool WL = decltype(with_lj)::value;
-        const unsigned sa = shared_addr(ring(grp, k) + 2 * jb) | ((unsigned)li << 5);
+        const unsigned sa = shared_addr(ring(grp, k) + 2 * jb);
+        auto at = [&](int t) { return sa | entry_off((unsigned)(li ^ t)); };
         float fx = 0.f, fy = 0.f, fz = 0.f, c_lj = 0.f, c_c = 0.f;
         float4 xa, aa, xb, ab;
-        lds128(sa, xa);
-        lds128(sa + 16u, aa);
+        lds128(at(0), xa);
+        lds128(at(0) ^ 16u, aa);
 #pragma unroll 1
         for (int t = 0; t < 8; t += 2) {
-            const unsigned o1 = sa ^ ((unsigned)(t + 1) << 5);
+            const unsigned o1 = at(t + 1);
             lds128(o1, xb);
-            lds128(o1 + 16u, ab);
+            lds128(o1 ^ 16u, ab);
             pair_interact<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, xi, pi, ik, lanebit, xa, aa,
                                                              fix, fiy, fiz, fx, fy, fz, c_lj, c_c,
                                                              n_in);
@@ -760,9 +771,9 @@ __device__ __forceinline__ void nb_item_q(const NbArgs &a, const int I, const in
             fy = __shfl_xor_sync(kFull, fy, 1);
             fz = __shfl_xor_sync(kFull, fz, 1);
             if (t < 6) {
-                const unsigned o2 = sa ^ ((unsigned)(t + 2) << 5);
+                const unsigned o2 = at(t + 2);
                 lds128(o2, xa);
-                lds128(o2 + 16u, aa);
+                lds128(o2 ^ 16u, aa);
             }
             pair_interact<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, xi, pi, ik, lanebit, xb, ab,
                                                              fix, fiy, fiz, fx, fy, fz, c_lj, c_c,
@@ -773,7 +784,7 @@ __device__ __forceinline__ void nb_item_q(const NbArgs &a, const int I, const in
             fz = __shfl_xor_sync(kFull, fz, m);
         }
         float4 own;
-        lds128((sa ^ (7u << 5)) + 16u, own);
+        lds128(at(7) ^ 16u, own);
         push_j(__float_as_int(own.w), fx, fy, fz);
         if (ENERGY) {
             acc_lj += (double)c_lj;
