@@ -422,3 +422,54 @@ def test_reference_binding_imports_the_installed_reference():
         partners = sorted(int(p) for p in t.bonded_particles[i] if p >= 0)
         m = i // 3
         assert partners == [j for j in range(3 * m, 3 * m + 3) if j != i]
+
+
+def test_bench_drift_statistics_and_gates():
+    """The NVE-drift estimator of bench.py on synthetic energy series: a
+    known slope under white noise is recovered within its standard error,
+    correlated (random-walk) noise widens the error instead of hiding in it,
+    and the gate requires |drift| + 2 sigma below the bar."""
+    import bench
+    from mdpy_gb300 import unit
+
+    rng = np.random.default_rng(4)
+    n_atoms = 1000
+    kt = unit.KB * bench.TEMPERATURE
+    t = np.arange(1, 5001) * 20.0                  # fs, a sample every 20 steps
+    true = 4e-4                                    # kT / ns / atom
+    slope = true * n_atoms * kt / 1e6              # energy per fs
+    white = slope * t + rng.normal(0.0, 5e-4 * n_atoms * kt, t.size)
+    d = bench.drift_statistics(t, white, n_atoms)
+    assert abs(d["kT_per_ns_per_atom"] - true) < 4 * d["stderr_kT_per_ns_per_atom"]
+    assert 0.5 <= d["autocorrelation_samples"] < 2.0
+    walk = slope * t + np.cumsum(rng.normal(0.0, 5e-5 * n_atoms * kt, t.size))
+    dw = bench.drift_statistics(t, walk, n_atoms)
+    assert dw["autocorrelation_samples"] > 20
+    assert dw["stderr_kT_per_ns_per_atom"] > 3 * d["stderr_kT_per_ns_per_atom"]
+    assert bench.drift_passes({"kT_per_ns_per_atom": 4e-4, "stderr_kT_per_ns_per_atom": 2e-4})
+    assert not bench.drift_passes({"kT_per_ns_per_atom": 4e-4, "stderr_kT_per_ns_per_atom": 4e-4})
+    assert not bench.drift_passes({"kT_per_ns_per_atom": -1.2e-3, "stderr_kT_per_ns_per_atom": 0.0})
+    assert not bench.drift_passes({"kT_per_ns_per_atom": None, "stderr_kT_per_ns_per_atom": None})
+    assert not bench.drift_passes(None)
+    assert bench.integrated_autocorrelation_time(np.zeros(10)) == 0.5
+
+
+def test_bench_reference_arm_runs_the_steps_it_reports():
+    """bench.py --impl reference on a small box: exactly --warmup + --steps
+    sampled steps, ms_per_step the measured sampled step, the whole-step time
+    extrapolated from it and said so."""
+    import json
+    import subprocess
+    import sys
+
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(repo, "bench.py"), "--impl", "reference",
+                          "--steps", "3", "--warmup", "1", "--waters", "300", "--box", "21",
+                          "--beads", "0", "--reference-seconds", "2"],
+                         capture_output=True, text=True, timeout=300, cwd=repo)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["steps"] == 3 and line["warmup"] == 1
+    assert line["ms_per_full_step_extrapolated"] >= line["ms_per_step"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and "extrapolated" in line["cpu_baseline"]["sample"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["value"] > 0
