@@ -48,6 +48,10 @@ struct NbArgs {
     int n_items;      // n_clusters * split
     int *queue;       // next item (zeroed before each persistent launch)
     int split_rings;  // 1: separate rings for LJ-carrying and charge-only j atoms
+    // the constants of the packed (two pairs per instruction) arithmetic, each
+    // float in both halves of a 64-bit word
+    unsigned long long pk_one, pk_a1, pk_a2, pk_a3, pk_a4, pk_a5, pk_bp, pk_negc, pk_fc, pk_k12,
+        pk_km6, pk_two, pk_rc2, pk_rs2, pk_krc, pk_swd;
 };
 
 namespace {
@@ -137,6 +141,198 @@ __device__ __forceinline__ void lds128(unsigned addr, float4 &v) {
     asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
                  : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
                  : "r"(addr));
+}
+
+// ---- two pairs per instruction -----------------------------------------
+// Blackwell's packed FP32 arithmetic (PTX add/mul/fma .f32x2): one
+// instruction computes the same operation on two independent (A, B) float
+// pairs held in a 64-bit register, each rounded as the scalar instruction
+// would.  The whole-warp sweep evaluates this lane's i atom against two j
+// atoms per step this way; special functions, compares and selects stay
+// scalar on the two halves.
+typedef unsigned long long u64;
+__device__ __forceinline__ u64 pk2(float a, float b) {
+    u64 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpk2(u64 r, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ u64 add2(u64 a, u64 b) {
+    u64 r;
+    asm("add.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
+    u64 r;
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
+    u64 r;
+    asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {  // a b + c
+    u64 r;
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ u64 neg2(u64 a) { return a ^ 0x8000000080000000ull; }
+__device__ __forceinline__ u64 splat2(float a) { return pk2(a, a); }
+__device__ __forceinline__ u64 lds64(unsigned addr) {
+    u64 v;
+    asm volatile("ld.shared.b64 %0, [%1];" : "=l"(v) : "r"(addr));
+    return v;
+}
+
+// the packed sweep loads each step's fields one step ahead (1) or at the
+// step (0)
+#ifndef MDG_PK_PREFETCH
+#define MDG_PK_PREFETCH 0
+#endif
+
+// Packed rings (whole-warp form): a ring of 128 atom slots is two
+// super-chunks of 64; a super-chunk holds eight field arrays of 32 (A, B)
+// pairs -- x, y, z, q, sigma/2, sqrt(4 eps), exclusion mask, slot -- 256
+// bytes each.  Atom slot p sits in pair p & 31, half (p >> 5) & 1, of
+// super-chunk p >> 6: the first 32 atoms of a super-chunk fill the A
+// halves, the next 32 the B halves.  A lane reads one 8-byte pair per field
+// and step; a quarter warp's eight lanes read eight pairs of one aligned
+// 64-byte block, so the loads are free of bank conflicts.
+constexpr int kPkRing = 128;   // atom slots per packed ring
+constexpr int kPkChunk = 512;  // floats per super-chunk
+__device__ __forceinline__ void put_entry_pk(float *ring, int p, float4 xq, float2 prm,
+                                             unsigned mask, int jk) {
+    float *w = ring + (p >> 6) * kPkChunk + (p & 31) * 2 + ((p >> 5) & 1);
+    w[0] = xq.x;
+    w[64] = xq.y;
+    w[128] = xq.z;
+    w[192] = xq.w;
+    w[256] = prm.x;
+    w[320] = prm.y;
+    w[384] = __uint_as_float(mask);
+    w[448] = __int_as_float(jk);
+}
+__device__ __forceinline__ void copy_entry_pk(const float *src, int ps, float *dst, int pd) {
+    const float *r = src + (ps >> 6) * kPkChunk + (ps & 31) * 2 + ((ps >> 5) & 1);
+    float *w = dst + (pd >> 6) * kPkChunk + (pd & 31) * 2 + ((pd >> 5) & 1);
+#pragma unroll
+    for (int f = 0; f < 8; ++f) w[64 * f] = r[64 * f];
+}
+
+// the lane's i atom, replicated into both halves
+struct PairI2 {
+    u64 X, Y, Z, Q, S, E;
+};
+
+// Two pairs at once: this lane's i atom with the (A, B) j atoms of one
+// packed step.  Same arithmetic as pair_interact, each operation applied to
+// both pairs.  FI accumulates +fr d (the i force is its negated sum of the
+// two halves); FJ the two j accumulators.
+template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool WL>
+__device__ __forceinline__ void pair_interact2(const NbArgs &a, const SysDev &sd,
+                                               const PairI2 &I2, int ik,
+                                               unsigned lanebit, u64 X, u64 Y, u64 Z, u64 Qj,
+                                               u64 Sj, u64 Ej, u64 M, u64 Jk, u64 &FIX, u64 &FIY,
+                                               u64 &FIZ, u64 &FJX, u64 &FJY, u64 &FJZ, u64 &CLJ,
+                                               u64 &CC, unsigned long long &n_in) {
+    const u64 DX = sub2(X, I2.X), DY = sub2(Y, I2.Y), DZ = sub2(Z, I2.Z);
+    const u64 R2 = fma2(DX, DX, fma2(DY, DY, mul2(DZ, DZ)));
+    float r2a, r2b, ma, mb;
+    unpk2(R2, r2a, r2b);
+    unpk2(M, ma, mb);
+    // masked and out-of-range pairs may compute inf/NaN; every use below
+    // selects them away
+    const bool inca = (r2a <= a.rc2) && !(__float_as_uint(ma) & lanebit);
+    const bool incb = (r2b <= a.rc2) && !(__float_as_uint(mb) & lanebit);
+    if (DUMP) {
+        float ja, jb;
+        unpk2(Jk, ja, jb);
+        const int pi_atom = a.perm[ik];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (h ? incb : inca) {
+                const int pj_atom = a.perm[__float_as_int(h ? jb : ja)];
+                if (ref_within32(a.x, pi_atom, pj_atom, sd, a.rc_ref)) {
+                    unsigned long long slot = atomicAdd(a.dump_count, 1ull);
+                    if ((long long)slot < a.dump_cap) {
+                        a.dump[2 * slot] = min(pi_atom, pj_atom);
+                        a.dump[2 * slot + 1] = max(pi_atom, pj_atom);
+                    }
+                }
+            }
+        }
+    }
+    const u64 RINV = pk2(rsqrtf(r2a), rsqrtf(r2b));
+    const u64 RINV2 = mul2(RINV, RINV);
+    u64 FR = 0ull, ELJ = 0ull, ECL = 0ull;
+    if (LJ && WL) {
+        const u64 SIG = add2(I2.S, Sj);
+        const u64 S2 = mul2(mul2(SIG, SIG), RINV2);
+        const u64 S6 = mul2(mul2(S2, S2), S2);
+        const u64 C6 = mul2(mul2(I2.E, Ej), S6);
+        u64 FLJ = mul2(mul2(C6, fma2(a.pk_k12, S6, a.pk_km6)), RINV2);
+        if (SWITCH) {
+            ELJ = mul2(C6, sub2(S6, a.pk_one));
+            float ua, ub;
+            unpk2(R2, ua, ub);
+            const u64 R2C = pk2(fmaxf(ua, a.rs2), fmaxf(ub, a.rs2));
+            const u64 U = sub2(a.pk_rc2, R2C);
+            const u64 SW = mul2(mul2(mul2(U, U), fma2(a.pk_two, R2C, a.pk_krc)), a.pk_swd);
+            const u64 DSW = mul2(mul2(a.pk_k12, U), mul2(sub2(a.pk_rs2, R2C), a.pk_swd));
+            FLJ = fma2(FLJ, SW, neg2(mul2(ELJ, DSW)));
+            ELJ = mul2(ELJ, SW);
+        } else if (ENERGY) {
+            ELJ = mul2(C6, sub2(S6, a.pk_one));
+        }
+        FR = FLJ;
+    }
+    if (COUL == MDG_COUL_EWALD) {
+        const u64 QQ = mul2(I2.Q, Qj);
+        const u64 R = mul2(R2, RINV);
+        float da, db;
+        unpk2(fma2(a.pk_bp, R, a.pk_one), da, db);
+        const u64 TT = pk2(fast_rcp(da), fast_rcp(db));
+        const u64 POLY =
+            mul2(TT, fma2(TT, fma2(TT, fma2(TT, fma2(TT, a.pk_a5, a.pk_a4), a.pk_a3), a.pk_a2), a.pk_a1));
+        float ea, eb;
+        unpk2(mul2(a.pk_negc, R2), ea, eb);
+        const u64 EX = pk2(fast_exp2(ea), fast_exp2(eb));
+        const u64 ECF = mul2(mul2(mul2(QQ, POLY), EX), RINV);
+        FR = fma2(fma2(mul2(QQ, a.pk_fc), EX, ECF), RINV2, FR);
+        if (ENERGY) {
+            float qa, qb, ra, rb, ia, ib;
+            unpk2(QQ, qa, qb);
+            unpk2(R, ra, rb);
+            unpk2(RINV, ia, ib);
+            ECL = pk2(qa * erfc_energy(a.beta * ra) * ia, qb * erfc_energy(a.beta * rb) * ib);
+        }
+    }
+    float fa, fb;
+    unpk2(FR, fa, fb);
+    FR = pk2(inca ? fa : 0.f, incb ? fb : 0.f);
+    FIX = fma2(FR, DX, FIX);
+    FIY = fma2(FR, DY, FIY);
+    FIZ = fma2(FR, DZ, FIZ);
+    FJX = fma2(FR, DX, FJX);
+    FJY = fma2(FR, DY, FJY);
+    FJZ = fma2(FR, DZ, FJZ);
+    if (ENERGY) {
+        float la, lb, ca, cb;
+        unpk2(ELJ, la, lb);
+        unpk2(ECL, ca, cb);
+        CLJ = add2(CLJ, pk2(inca ? la : 0.f, incb ? lb : 0.f));
+        CC = add2(CC, pk2(inca ? ca : 0.f, incb ? cb : 0.f));
+        n_in += __popc(__ballot_sync(kFull, inca)) + __popc(__ballot_sync(kFull, incb));
+    }
+}
+
+__device__ __forceinline__ u64 shfl_xor2(u64 v, unsigned m) {
+    float a, b;
+    unpk2(v, a, b);
+    return pk2(__shfl_xor_sync(kFull, a, m), __shfl_xor_sync(kFull, b, m));
 }
 
 // One pair: this lane's i atom (xi: position and scaled charge; pi: sigma/2
@@ -426,6 +622,17 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
 
     float fix = 0.f, fiy = 0.f, fiz = 0.f;
     double acc_lj = 0.0, acc_c = 0.0;  // per-lane energies: FP32 within a chunk, FP64 across
+    // whole warp: the packed rings, this lane's i atom in both halves, the
+    // packed constants and the packed i-force sums (+fr d, negated at the end)
+    float *const pringL = (float *)s_j, *const pringQ = (float *)s_j + 2 * kPkChunk;
+    PairI2 I2;
+    I2.X = splat2(xi.x);
+    I2.Y = splat2(xi.y);
+    I2.Z = splat2(xi.z);
+    I2.Q = splat2(xi.w);
+    I2.S = splat2(pi.x);
+    I2.E = splat2(pi.y);
+    u64 FIX = 0ull, FIY = 0ull, FIZ = 0ull;
     unsigned long long n_eval = 0, n_in = 0;
     // two rings: j atoms with LJ parameters, and charge-only j atoms, whose
     // sweeps skip the LJ arithmetic (two of every three water atoms)
@@ -501,6 +708,88 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         __syncwarp();
     };
     auto shared_addr = [](const float4 *p) { return (unsigned)__cvta_generic_to_shared(p); };
+    auto shared_addr_f = [](const float *p) { return (unsigned)__cvta_generic_to_shared(p); };
+    auto push_j = [&](int jk, float fjx, float fjy, float fjz) {
+        if (jk >= 0 && !DUMP) {
+            if (!(fabsf(fjx) < kFixLimit && fabsf(fjy) < kFixLimit && fabsf(fjz) < kFixLimit))
+                raise_status(a.status, MDG_ERR_OVERFLOW);
+            fix_red(&a.f[jk], to_fix(fjx));
+            fix_red(&a.f[a.n_pad + jk], to_fix(fjy));
+            fix_red(&a.f[2 * a.n_pad + jk], to_fix(fjz));
+        }
+    };
+    // Whole warp: one packed super-chunk (64 j atoms as 32 (A, B) pairs) at
+    // byte address sa, swept in 32 rotation steps: at step t lane l pairs its
+    // i atom with pair l ^ t (both halves at once), the pair's j-force
+    // accumulators travel by butterfly shuffles (mask t ^ (t + 1)), and
+    // after step 31 lane l owns pair l ^ 31's two j forces.  Each step's
+    // fields are loaded one step ahead.
+    auto chunk64 = [&](auto with_lj, unsigned sa) {
+        constexpr bool WL = decltype(with_lj)::value;
+        u64 FJX = 0ull, FJY = 0ull, FJZ = 0ull, CLJ = 0ull, CC = 0ull;
+        auto load = [&](int t, u64 &X, u64 &Y, u64 &Z, u64 &Q, u64 &S, u64 &E, u64 &M, u64 &J) {
+            const unsigned ad = sa + ((unsigned)(lane ^ t) << 3);
+            X = lds64(ad);
+            Y = lds64(ad + 256u);
+            Z = lds64(ad + 512u);
+            Q = lds64(ad + 768u);
+            S = (LJ && WL) ? lds64(ad + 1024u) : 0ull;
+            E = (LJ && WL) ? lds64(ad + 1280u) : 0ull;
+            M = lds64(ad + 1536u);
+            J = DUMP ? lds64(ad + 1792u) : 0ull;
+        };
+#if MDG_PK_PREFETCH
+        u64 X0, Y0, Z0, Q0, S0, E0, M0, J0, X1, Y1, Z1, Q1, S1, E1, M1, J1;
+        load(0, X0, Y0, Z0, Q0, S0, E0, M0, J0);
+#pragma unroll 1
+        for (int t = 0; t < 32; t += 2) {
+            load(t + 1, X1, Y1, Z1, Q1, S1, E1, M1, J1);
+            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, ik, lanebit, X0, Y0,
+                                                              Z0, Q0, S0, E0, M0, J0, FIX, FIY,
+                                                              FIZ, FJX, FJY, FJZ, CLJ, CC, n_in);
+            FJX = shfl_xor2(FJX, 1u);
+            FJY = shfl_xor2(FJY, 1u);
+            FJZ = shfl_xor2(FJZ, 1u);
+            if (t < 30) load(t + 2, X0, Y0, Z0, Q0, S0, E0, M0, J0);
+            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, ik, lanebit, X1, Y1,
+                                                              Z1, Q1, S1, E1, M1, J1, FIX, FIY,
+                                                              FIZ, FJX, FJY, FJZ, CLJ, CC, n_in);
+            const unsigned m = t < 30 ? (unsigned)((t + 1) ^ (t + 2)) : 0u;
+            FJX = shfl_xor2(FJX, m);
+            FJY = shfl_xor2(FJY, m);
+            FJZ = shfl_xor2(FJZ, m);
+        }
+#else
+#pragma unroll 2
+        for (int t = 0; t < 32; ++t) {
+            u64 X, Y, Z, Q, S, E, M, J;
+            load(t, X, Y, Z, Q, S, E, M, J);
+            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, ik, lanebit, X, Y, Z, Q,
+                                                              S, E, M, J, FIX, FIY, FIZ, FJX,
+                                                              FJY, FJZ, CLJ, CC, n_in);
+            const unsigned m = t < 31 ? (unsigned)(t ^ (t + 1)) : 0u;
+            FJX = shfl_xor2(FJX, m);
+            FJY = shfl_xor2(FJY, m);
+            FJZ = shfl_xor2(FJZ, m);
+        }
+#endif
+        float ja, jb, xa, xb, ya, yb, za, zb;
+        unpk2(lds64(sa + ((unsigned)(lane ^ 31) << 3) + 1792u), ja, jb);
+        unpk2(FJX, xa, xb);
+        unpk2(FJY, ya, yb);
+        unpk2(FJZ, za, zb);
+        push_j(__float_as_int(ja), xa, ya, za);
+        push_j(__float_as_int(jb), xb, yb, zb);
+        if (ENERGY) {
+            float p0, p1, q0, q1;
+            unpk2(CLJ, p0, p1);
+            unpk2(CC, q0, q1);
+            acc_lj += (double)p0 + (double)p1;
+            acc_c += (double)q0 + (double)q1;
+        }
+        n_eval += 2048;
+        __syncwarp();
+    };
 
     // HALF mode: one 16-step sweep of up to 16 entries of each half's ring of
     // one kind; a half with fewer pending entries is padded with far-away ones
@@ -600,21 +889,26 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         if ((bL | bQ) == 0u) return;
         if (hitL || hitQ) {
             const unsigned m = excl_mask();
-            if (hitL) put_entry(ringL, (jbL + jcL + __popc(bL & lt)) & (kRing - 1), xj, pj, m, jk);
-            else put_entry(ringQ, (jbQ + jcQ + __popc(bQ & lt)) & (kRing - 1), xj, pj, m, jk);
+            if (hitL)
+                put_entry_pk(pringL, (jbL + jcL + __popc(bL & lt)) & (kPkRing - 1), xj, pj, m, jk);
+            else
+                put_entry_pk(pringQ, (jbQ + jcQ + __popc(bQ & lt)) & (kPkRing - 1), xj, pj, m, jk);
         }
         jcL += __popc(bL);
         jcQ += __popc(bQ);
         __syncwarp();
-        if (jcL >= 32) {
-            chunk(std::true_type{}, std::integral_constant<int, 32>{}, shared_addr(ringL + 2 * jbL));
-            jbL = (jbL + 32) & (kRing - 1);
-            jcL -= 32;
+        // a full super-chunk of a ring is swept; between candidates a ring
+        // holds fewer than 64 pending slots (a candidate adds at most 32, so
+        // never more than 95 of 128)
+        if (jcL >= 64) {
+            chunk64(std::true_type{}, shared_addr_f(pringL + (jbL >> 6) * kPkChunk));
+            jbL = (jbL + 64) & (kPkRing - 1);
+            jcL -= 64;
         }
-        if (jcQ >= 32) {
-            chunk(std::false_type{}, std::integral_constant<int, 32>{}, shared_addr(ringQ + 2 * jbQ));
-            jbQ = (jbQ + 32) & (kRing - 1);
-            jcQ -= 32;
+        if (jcQ >= 64) {
+            chunk64(std::false_type{}, shared_addr_f(pringQ + (jbQ >> 6) * kPkChunk));
+            jbQ = (jbQ + 64) & (kPkRing - 1);
+            jcQ -= 64;
         }
     };
 
@@ -640,26 +934,36 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         while (jcL > 0 || jcL2 > 0) sweep16(std::true_type{});
         while (jcQ > 0 || jcQ2 > 0) sweep16(std::false_type{});
     }
-    if (!HALF && jcQ > 0 && jcL + jcQ <= 32) {
-        if (lane < jcQ)
-            copy_entry(ringQ, (jbQ + lane) & (kRing - 1), ringL, (jbL + jcL + lane) & (kRing - 1));
-        jcL += jcQ;
-        jcQ = 0;
-        __syncwarp();
-    }
-    if (!HALF && jcL > 0) {
-        if (lane >= jcL)
-            put_entry(ringL, (jbL + lane) & (kRing - 1), make_float4(kFarAway, kFarAway, kFarAway, 0.f),
-                      make_float2(0.f, 0.f), kFull, -1);
-        __syncwarp();
-        chunk(std::true_type{}, std::integral_constant<int, 32>{}, shared_addr(ringL + 2 * jbL));
-    }
-    if (!HALF && jcQ > 0) {
-        if (lane >= jcQ)
-            put_entry(ringQ, (jbQ + lane) & (kRing - 1), make_float4(kFarAway, kFarAway, kFarAway, 0.f),
-                      make_float2(0.f, 0.f), kFull, -1);
-        __syncwarp();
-        chunk(std::false_type{}, std::integral_constant<int, 32>{}, shared_addr(ringQ + 2 * jbQ));
+    if constexpr (!HALF) {
+        // the partial super-chunks: charge-only slots join the LJ ring when
+        // both fit in one (their LJ terms are zero), then each partial one is
+        // padded with far-away slots up to 64 and swept
+        if (jcQ > 0 && jcL + jcQ <= 64) {
+            for (int k = lane; k < jcQ; k += 32)
+                copy_entry_pk(pringQ, (jbQ + k) & (kPkRing - 1), pringL,
+                              (jbL + jcL + k) & (kPkRing - 1));
+            jcL += jcQ;
+            jcQ = 0;
+            __syncwarp();
+        }
+        auto finish = [&](auto with_lj, float *ring, int jb, int jc) {
+            if (jc == 0) return;
+            for (int k = jc + lane; k < 64; k += 32)
+                put_entry_pk(ring, (jb + k) & (kPkRing - 1),
+                             make_float4(kFarAway, kFarAway, kFarAway, 0.f), make_float2(0.f, 0.f),
+                             kFull, -1);
+            __syncwarp();
+            chunk64(with_lj, shared_addr_f(ring + (jb >> 6) * kPkChunk));
+        };
+        finish(std::true_type{}, pringL, jbL, jcL);
+        finish(std::false_type{}, pringQ, jbQ, jcQ);
+        float a0, a1, b0, b1, c0, c1;
+        unpk2(FIX, a0, a1);
+        unpk2(FIY, b0, b1);
+        unpk2(FIZ, c0, c1);
+        fix -= a0 + a1;
+        fiy -= b0 + b1;
+        fiz -= c0 + c1;
     }
 
     // ---- this work item's share of the i forces and energies -------------
@@ -937,16 +1241,22 @@ __global__ void __launch_bounds__(32, ENERGY ? 12 : 13) k_nonbonded_q(NbArgs a) 
 // Grid form: one one-warp CTA per work item, scheduled by the hardware.
 // Persistent form: enough warps to fill the GPU once, each pulling work
 // items from a device counter until none is left.
-// resident one-warp CTAs per SM the register budget is sized for (96
-// registers at 20)
+// resident one-warp CTAs per SM the register budget is sized for: the
+// packed whole-warp sweep needs 128 registers (16 CTAs; its energy variant
+// up to 170, 12 CTAs), the half-warp form 96 (20)
 #ifndef MDG_NB_MIN_BLOCKS
-#define MDG_NB_MIN_BLOCKS 20
+#define MDG_NB_MIN_BLOCKS 16
+#endif
+#ifndef MDG_NB_MIN_BLOCKS_HALF
+#define MDG_NB_MIN_BLOCKS_HALF 20
 #endif
 template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool HALF>
-__global__ void __launch_bounds__(32, ENERGY ? 16 : MDG_NB_MIN_BLOCKS) k_nonbonded(NbArgs a) {
+__global__ void __launch_bounds__(32, ENERGY ? (HALF ? 16 : 12)
+                                             : (HALF ? MDG_NB_MIN_BLOCKS_HALF : MDG_NB_MIN_BLOCKS))
+    k_nonbonded(NbArgs a) {
     // two rings of 64 entries of 32 bytes; each 32-entry chunk starts on a
     // 1024-byte boundary
-    __shared__ __align__(1024) float4 s_j[(HALF ? 8 : 4) * kRing];
+    __shared__ __align__(1024) float4 s_j[8 * kRing];
     if (!a.persistent) {
         nb_item<COUL, LJ, SWITCH, ENERGY, DUMP, HALF>(a, blockIdx.x / a.split, blockIdx.x % a.split,
                                                 s_j);
