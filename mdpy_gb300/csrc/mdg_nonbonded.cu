@@ -33,8 +33,6 @@
 // bit-reproducible run to run.  Pairs are never stored: the pair set is
 // found afresh from the current coordinates on every evaluation, so no
 // Verlet skin or rebuild criterion exists that could miss a pair.
-#include <cstring>
-
 #include "mdg_nonbonded_kernel.cuh"
 
 namespace mdg {
@@ -221,33 +219,6 @@ __global__ void k_special(SpArgs a) {
     block_energy_add<3>(a.energy, sid, v, slot);
 }
 
-// a float in both halves of a 64-bit word (the packed arithmetic's operands)
-unsigned long long pk_bits(float v) {
-    unsigned u;
-    std::memcpy(&u, &v, sizeof(u));
-    return ((unsigned long long)u << 32) | u;
-}
-
-// the packed constants, from the final values of the scalar ones
-void set_packed_constants(NbArgs &a) {
-    a.pk_one = pk_bits(1.0f);
-    a.pk_a1 = pk_bits(kAsA1);
-    a.pk_a2 = pk_bits(kAsA2);
-    a.pk_a3 = pk_bits(kAsA3);
-    a.pk_a4 = pk_bits(kAsA4);
-    a.pk_a5 = pk_bits(kAsA5);
-    a.pk_bp = pk_bits(a.beta_p);
-    a.pk_negc = pk_bits(-a.ewald_exp_c);
-    a.pk_fc = pk_bits(a.ewald_fc);
-    a.pk_k12 = pk_bits(12.0f);
-    a.pk_km6 = pk_bits(-6.0f);
-    a.pk_two = pk_bits(2.0f);
-    a.pk_rc2 = pk_bits(a.rc2);
-    a.pk_rs2 = pk_bits(a.rs2);
-    a.pk_krc = pk_bits(a.rc2 - 3.0f * a.rs2);
-    a.pk_swd = pk_bits(a.sw_inv_den);
-}
-
 NbArgs make_args(mdg_system *s) {
     NbArgs a;
     a.xq = s->xq;
@@ -315,7 +286,6 @@ cudaError_t launch_nonbonded(mdg_system *s, unsigned mask, int energy, int dump)
         a.rc = s->cutoff + kDumpMargin;
         a.rc2 = a.rc * a.rc;
     }
-    set_packed_constants(a);
     const bool sw = s->rswitch > 0 && s->rswitch < s->cutoff;
     cudaError_t err = cudaSuccess;
     const int coul_tile = (want_c && s->coul_mode == MDG_COUL_EWALD) ? MDG_COUL_EWALD : MDG_COUL_NONE;

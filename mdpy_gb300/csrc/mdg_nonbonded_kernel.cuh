@@ -48,10 +48,6 @@ struct NbArgs {
     int n_items;      // n_clusters * split
     int *queue;       // next item (zeroed before each persistent launch)
     int split_rings;  // 1: separate rings for LJ-carrying and charge-only j atoms
-    // the constants of the packed (two pairs per instruction) arithmetic, each
-    // float in both halves of a 64-bit word
-    unsigned long long pk_one, pk_a1, pk_a2, pk_a3, pk_a4, pk_a5, pk_bp, pk_negc, pk_fc, pk_k12,
-        pk_km6, pk_two, pk_rc2, pk_rs2, pk_krc, pk_swd;
 };
 
 namespace {
@@ -226,6 +222,9 @@ __device__ __forceinline__ void copy_entry_pk(const float *src, int ps, float *d
 struct PairI2 {
     u64 X, Y, Z, Q, S, E;
 };
+struct PkC {
+    u64 one, six, a1, a2, a3, a4, a5, fc, swd, swd12;
+};
 
 // Two pairs at once: this lane's i atom with the (A, B) j atoms of one
 // packed step.  Same arithmetic as pair_interact, each operation applied to
@@ -233,7 +232,7 @@ struct PairI2 {
 // two halves); FJ the two j accumulators.
 template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool WL>
 __device__ __forceinline__ void pair_interact2(const NbArgs &a, const SysDev &sd,
-                                               const PairI2 &I2, int ik,
+                                               const PairI2 &I2, const PkC &c, int ik,
                                                unsigned lanebit, u64 X, u64 Y, u64 Z, u64 Qj,
                                                u64 Sj, u64 Ej, u64 M, u64 Jk, u64 &FIX, u64 &FIY,
                                                u64 &FIZ, u64 &FJX, u64 &FJY, u64 &FJZ, u64 &CLJ,
@@ -273,39 +272,48 @@ __device__ __forceinline__ void pair_interact2(const NbArgs &a, const SysDev &sd
         const u64 S2 = mul2(mul2(SIG, SIG), RINV2);
         const u64 S6 = mul2(mul2(S2, S2), S2);
         const u64 C6 = mul2(mul2(I2.E, Ej), S6);
-        u64 FLJ = mul2(mul2(C6, fma2(a.pk_k12, S6, a.pk_km6)), RINV2);
+        // 24 eps (2 s^12 - s^6) / r^2 with c6 = 4 eps s^6: c6 (12 s6 - 6) / r^2
+        const u64 C6X6 = mul2(C6, c.six);
+        u64 FLJ = mul2(mul2(C6X6, sub2(add2(S6, S6), c.one)), RINV2);
         if (SWITCH) {
-            ELJ = mul2(C6, sub2(S6, a.pk_one));
+            ELJ = mul2(C6, sub2(S6, c.one));
+            // the range terms on the scalar halves (constants from the
+            // arguments): r2c = max(r^2, rs^2), rc^2 - r2c, rc^2 + 2 r2c -
+            // 3 rs^2, rs^2 - r2c
             float ua, ub;
             unpk2(R2, ua, ub);
-            const u64 R2C = pk2(fmaxf(ua, a.rs2), fmaxf(ub, a.rs2));
-            const u64 U = sub2(a.pk_rc2, R2C);
-            const u64 SW = mul2(mul2(mul2(U, U), fma2(a.pk_two, R2C, a.pk_krc)), a.pk_swd);
-            const u64 DSW = mul2(mul2(a.pk_k12, U), mul2(sub2(a.pk_rs2, R2C), a.pk_swd));
+            ua = fmaxf(ua, a.rs2);
+            ub = fmaxf(ub, a.rs2);
+            const float krc = a.rc2 - 3.0f * a.rs2;
+            const u64 U = pk2(a.rc2 - ua, a.rc2 - ub);
+            const u64 W = pk2(fmaf(2.0f, ua, krc), fmaf(2.0f, ub, krc));
+            const u64 V = pk2(a.rs2 - ua, a.rs2 - ub);
+            const u64 SW = mul2(mul2(mul2(U, U), W), c.swd);
+            const u64 DSW = mul2(mul2(U, V), c.swd12);
             FLJ = fma2(FLJ, SW, neg2(mul2(ELJ, DSW)));
             ELJ = mul2(ELJ, SW);
         } else if (ENERGY) {
-            ELJ = mul2(C6, sub2(S6, a.pk_one));
+            ELJ = mul2(C6, sub2(S6, c.one));
         }
         FR = FLJ;
     }
     if (COUL == MDG_COUL_EWALD) {
         const u64 QQ = mul2(I2.Q, Qj);
-        const u64 R = mul2(R2, RINV);
-        float da, db;
-        unpk2(fma2(a.pk_bp, R, a.pk_one), da, db);
-        const u64 TT = pk2(fast_rcp(da), fast_rcp(db));
+        float ra, rb, sa2, sb2;
+        unpk2(RINV, ra, rb);
+        unpk2(R2, sa2, sb2);
+        ra *= sa2;  // r = r^2 / r
+        rb *= sb2;
+        // the scalar halves take the constants straight from the arguments
+        const u64 TT = pk2(fast_rcp(fmaf(a.beta_p, ra, 1.0f)), fast_rcp(fmaf(a.beta_p, rb, 1.0f)));
+        const u64 EX = pk2(fast_exp2(-a.ewald_exp_c * sa2), fast_exp2(-a.ewald_exp_c * sb2));
         const u64 POLY =
-            mul2(TT, fma2(TT, fma2(TT, fma2(TT, fma2(TT, a.pk_a5, a.pk_a4), a.pk_a3), a.pk_a2), a.pk_a1));
-        float ea, eb;
-        unpk2(mul2(a.pk_negc, R2), ea, eb);
-        const u64 EX = pk2(fast_exp2(ea), fast_exp2(eb));
-        const u64 ECF = mul2(mul2(mul2(QQ, POLY), EX), RINV);
-        FR = fma2(fma2(mul2(QQ, a.pk_fc), EX, ECF), RINV2, FR);
+            mul2(TT, fma2(TT, fma2(TT, fma2(TT, fma2(TT, c.a5, c.a4), c.a3), c.a2), c.a1));
+        // q q e^{-b^2 r^2} (erfc-fit/r + 2 b/sqrt(pi)) / r^2
+        FR = fma2(mul2(mul2(QQ, EX), fma2(POLY, RINV, c.fc)), RINV2, FR);
         if (ENERGY) {
-            float qa, qb, ra, rb, ia, ib;
+            float qa, qb, ia, ib;
             unpk2(QQ, qa, qb);
-            unpk2(R, ra, rb);
             unpk2(RINV, ia, ib);
             ECL = pk2(qa * erfc_energy(a.beta * ra) * ia, qb * erfc_energy(a.beta * rb) * ib);
         }
@@ -632,6 +640,17 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
     I2.Q = splat2(xi.w);
     I2.S = splat2(pi.x);
     I2.E = splat2(pi.y);
+    PkC pc;
+    pc.one = splat2(1.0f);
+    pc.six = splat2(6.0f);
+    pc.a1 = splat2(kAsA1);
+    pc.a2 = splat2(kAsA2);
+    pc.a3 = splat2(kAsA3);
+    pc.a4 = splat2(kAsA4);
+    pc.a5 = splat2(kAsA5);
+    pc.fc = splat2(a.ewald_fc);
+    pc.swd = splat2(a.sw_inv_den);
+    pc.swd12 = splat2(12.0f * a.sw_inv_den);
     u64 FIX = 0ull, FIY = 0ull, FIZ = 0ull;
     unsigned long long n_eval = 0, n_in = 0;
     // two rings: j atoms with LJ parameters, and charge-only j atoms, whose
@@ -744,14 +763,14 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
 #pragma unroll 1
         for (int t = 0; t < 32; t += 2) {
             load(t + 1, X1, Y1, Z1, Q1, S1, E1, M1, J1);
-            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, ik, lanebit, X0, Y0,
+            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, pc, ik, lanebit, X0, Y0,
                                                               Z0, Q0, S0, E0, M0, J0, FIX, FIY,
                                                               FIZ, FJX, FJY, FJZ, CLJ, CC, n_in);
             FJX = shfl_xor2(FJX, 1u);
             FJY = shfl_xor2(FJY, 1u);
             FJZ = shfl_xor2(FJZ, 1u);
             if (t < 30) load(t + 2, X0, Y0, Z0, Q0, S0, E0, M0, J0);
-            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, ik, lanebit, X1, Y1,
+            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, pc, ik, lanebit, X1, Y1,
                                                               Z1, Q1, S1, E1, M1, J1, FIX, FIY,
                                                               FIZ, FJX, FJY, FJZ, CLJ, CC, n_in);
             const unsigned m = t < 30 ? (unsigned)((t + 1) ^ (t + 2)) : 0u;
@@ -764,7 +783,7 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         for (int t = 0; t < 32; ++t) {
             u64 X, Y, Z, Q, S, E, M, J;
             load(t, X, Y, Z, Q, S, E, M, J);
-            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, ik, lanebit, X, Y, Z, Q,
+            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, pc, ik, lanebit, X, Y, Z, Q,
                                                               S, E, M, J, FIX, FIY, FIZ, FJX,
                                                               FJY, FJZ, CLJ, CC, n_in);
             const unsigned m = t < 31 ? (unsigned)(t ^ (t + 1)) : 0u;
@@ -1241,17 +1260,16 @@ __global__ void __launch_bounds__(32, ENERGY ? 12 : 13) k_nonbonded_q(NbArgs a) 
 // Grid form: one one-warp CTA per work item, scheduled by the hardware.
 // Persistent form: enough warps to fill the GPU once, each pulling work
 // items from a device counter until none is left.
-// resident one-warp CTAs per SM the register budget is sized for: the
-// packed whole-warp sweep needs 128 registers (16 CTAs; its energy variant
-// up to 170, 12 CTAs), the half-warp form 96 (20)
+// resident one-warp CTAs per SM the register budget is sized for (96
+// registers at 20; the energy variants 128 at 16)
 #ifndef MDG_NB_MIN_BLOCKS
-#define MDG_NB_MIN_BLOCKS 16
+#define MDG_NB_MIN_BLOCKS 20
 #endif
 #ifndef MDG_NB_MIN_BLOCKS_HALF
 #define MDG_NB_MIN_BLOCKS_HALF 20
 #endif
 template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool HALF>
-__global__ void __launch_bounds__(32, ENERGY ? (HALF ? 16 : 12)
+__global__ void __launch_bounds__(32, ENERGY ? 16
                                              : (HALF ? MDG_NB_MIN_BLOCKS_HALF : MDG_NB_MIN_BLOCKS))
     k_nonbonded(NbArgs a) {
     // two rings of 64 entries of 32 bytes; each 32-entry chunk starts on a
