@@ -18,9 +18,10 @@ slow force with PME every k steps (--learned; trained first on frame pairs
 of a plain Langevin run at 280-320 K).  Every form, plain included, is gated
 twice: the force the integrator applies on each step of one outer cycle
 must lie within 1e-4 relative RMS of the FP64 force at the same positions
-(largest over the cycle), and its NVE energy drift over 100 ps (after one
-shared Langevin equilibration) must satisfy |drift| + 2 sigma <= 1e-3
-kT/ns/atom.  "chosen" is the fastest form that passes both.
+(largest over the cycle), and its NVE energy drift (after one shared
+Langevin equilibration; 200 ps for the forms that pass the force gate,
+100 ps for the others) must satisfy |drift| + 2 sigma <= 1e-3 kT/ns/atom.
+"chosen" is the fastest form that passes both.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -112,6 +113,10 @@ def parse():
     p.add_argument("--nve-ps", type=float, default=None,
                    help="velocity-Verlet NVE run after the timed region for the energy drift "
                         "(default 100 ps on water90k, 0 elsewhere)")
+    p.add_argument("--nve-ps-eligible", type=float, default=200.0,
+                   help="NVE window of the forms that passed the force gate (the ones that "
+                        "can be chosen): 100 ps resolves the drift only to a few 1e-4 "
+                        "kT/ns/atom run to run, against a 1e-3 bar on |drift| + 2 sigma")
     a = p.parse_args()
     w, b, beads, grid = WORKLOADS.get(a.workload, WORKLOADS["water90k"])
     a.waters = w if a.waters is None else a.waters
@@ -1071,8 +1076,13 @@ def main():
         for f in [plain] + forms:
             sysm.set_positions(x_eq)
             sysm.set_velocities(v_eq)
+            # a form that can be chosen (force gate passed) gets the longer
+            # window; the others' drift is reported from the shorter one
+            fe = f.get("force_error")
+            ps = (max(a.nve_ps, a.nve_ps_eligible)
+                  if fe is not None and fe["max"] <= FORCE_BAR else a.nve_ps)
             try:
-                f["nve_drift"] = nve_drift(sysm, mask, n, a.nve_ps, mts=f.get("mts", 1),
+                f["nve_drift"] = nve_drift(sysm, mask, n, ps, mts=f.get("mts", 1),
                                            learned=learned_forms.get(id(f)))
                 f["nve_drift"]["equilibration"] = "%g ps Langevin at 300 K (%.0f s), shared" % (
                     a.equilibrate_ps, t_eq)
