@@ -169,6 +169,27 @@ MDG_API int mdg_get_energies(mdg_system *sys, double *energies, double *kinetic)
 /* Ensemble._update_kinetic_energy (mdpy/ensemble.py:63-71), FP64 */
 MDG_API int mdg_kinetic_energy(mdg_system *sys, double *kinetic);
 
+/* Energy snapshots for log dumping without a host synchronisation per dump:
+ * the device->host half of LogDumper.dump (mdpy/dumper/log_dumper.py:
+ * 105-208, which reads Ensemble energies as Simulation.integrate reaches
+ * each dump step, mdpy/simulation.py:60-70).  mdg_energy_snapshot enqueues
+ * on the system's stream a copy of the energy words of the last evaluation
+ * with energies (and of the device status word) into pinned ring slot `slot`
+ * (0 <= slot < MDG_SNAPSHOT_SLOTS, allocated on first use) and records an
+ * event; it returns without waiting, so the steps enqueued after it keep the
+ * GPU busy while the host formats earlier rows.  mdg_energy_snapshot_read
+ * turns slot `slot` into energies[MDG_NUM_TERMS] and *kinetic exactly as
+ * mdg_get_energies would have at the snapshot: with wait != 0 it waits for
+ * the copy; with wait == 0 it sets *ready = 0 and leaves the outputs alone
+ * if the copy has not completed yet (*ready = 1 otherwise; ready may be
+ * NULL when wait != 0).  A device error raised before the snapshot (particle
+ * loss, fixed-point overflow) is returned by the read.  Reusing a slot
+ * before its read overwrites it. */
+#define MDG_SNAPSHOT_SLOTS 8
+MDG_API int mdg_energy_snapshot(mdg_system *sys, int slot);
+MDG_API int mdg_energy_snapshot_read(mdg_system *sys, int slot, int wait, double *energies,
+                                     double *kinetic, int *ready);
+
 /* One call for a host-driven loop (no reference counterpart; it bundles
  * State.set_positions/set_velocities, Integrator.integrate and the reads of
  * State.positions/velocities and the energies): copies x_in / v_in (host,

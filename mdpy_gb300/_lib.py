@@ -24,6 +24,7 @@ TERM_NAMES = ("lj", "coulomb_real", "coulomb_recip", "bond", "angle", "dihedral"
 COUL_NONE, COUL_EWALD, COUL_BARE = 0, 1, 2
 INTEGRATOR_VERLET, INTEGRATOR_LANGEVIN = 0, 1
 MASK_ALL = (1 << NUM_TERMS) - 1
+SNAPSHOT_SLOTS = 8
 
 
 def mask(*terms):
@@ -74,6 +75,8 @@ SIGNATURES = {
     "mdg_get_forces": [_sys_p, ctypes.c_void_p, ctypes.c_int],
     "mdg_get_energies": [_sys_p, _c_dbl_p, _c_dbl_p],
     "mdg_kinetic_energy": [_sys_p, _c_dbl_p],
+    "mdg_energy_snapshot": [_sys_p, ctypes.c_int],
+    "mdg_energy_snapshot_read": [_sys_p, ctypes.c_int, ctypes.c_int, _c_dbl_p, _c_dbl_p, _c_int_p],
     "mdg_kinetic_energies_noalloc": [_sys_p, _c_dbl_p],
     "mdg_minimize_step": [_sys_p, ctypes.c_double],
     "mdg_set_mts": [_sys_p, ctypes.c_int],
@@ -328,6 +331,21 @@ class System:
         ke = ctypes.c_double(0.0)
         check(self._lib.mdg_get_energies(self._h, _dp(e), ctypes.byref(ke)))
         return e, ke.value
+
+    def energy_snapshot(self, slot):
+        """Enqueue a copy of the current energies into pinned slot ``slot``
+        (no synchronisation)."""
+        check(self._lib.mdg_energy_snapshot(self._h, int(slot)))
+
+    def energy_snapshot_read(self, slot, wait=True):
+        """(energies, kinetic) of snapshot ``slot``; with ``wait=False``
+        None if its copy has not completed yet."""
+        e = np.zeros(NUM_TERMS)
+        ke = ctypes.c_double(0.0)
+        ready = ctypes.c_int(0)
+        check(self._lib.mdg_energy_snapshot_read(self._h, int(slot), 1 if wait else 0, _dp(e),
+                                                 ctypes.byref(ke), ctypes.byref(ready)))
+        return (e, ke.value) if ready.value else None
 
     SHAPE_FIELDS = ("split", "persistent", "pme_block", "side_priority", "split_rings",
                     "pme_tiles", "half")

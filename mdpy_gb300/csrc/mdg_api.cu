@@ -555,6 +555,9 @@ MDG_API int mdg_system_destroy(mdg_system *s) {
     if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     if (s->host_stage) cudaFreeHost(s->host_stage);
+    for (cudaEvent_t &ev : s->snap_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (s->snap_host) cudaFreeHost(s->snap_host);
     dfree(s->xin);
     dfree(s->vsave);
     dfree(s->same_flag);
@@ -1017,6 +1020,86 @@ MDG_API int mdg_get_energies_batch(mdg_system *s, double *energies, double *kine
         }
         if (kinetic) kinetic[q] = (double)eq[kSlotKinetic] * kFixInv;
     }
+    return MDG_OK;
+}
+
+namespace {
+// energy words + status word of one snapshot slot
+size_t snap_words(const mdg_system *s) { return (size_t)kEnergySlots * s->n_sys + 1; }
+
+// energies[MDG_NUM_TERMS] (sums over the batch) and the kinetic energy from
+// kEnergySlots * n_sys fixed-point words, as mdg_get_energies reports them
+void energies_from_words(const mdg_system *s, const long long *e, bool recip, double *energies,
+                         double *kinetic) {
+    if (energies)
+        for (int t = 0; t < MDG_NUM_TERMS; ++t) {
+            double a = 0.0;
+            for (int q = 0; q < s->n_sys; ++q) {
+                a += (double)e[(size_t)kEnergySlots * q + t] * kFixInv;
+                if (recip && t == MDG_TERM_COUL_RECIP) a += s->e_self[q] + s->e_net[q];
+            }
+            energies[t] = a;
+        }
+    if (kinetic) {
+        double a = 0.0;
+        for (int q = 0; q < s->n_sys; ++q) a += (double)e[(size_t)kEnergySlots * q + kSlotKinetic] * kFixInv;
+        *kinetic = a;
+    }
+}
+}  // namespace
+
+MDG_API int mdg_energy_snapshot(mdg_system *s, int slot) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (slot < 0 || slot >= MDG_SNAPSHOT_SLOTS)
+        return fail(MDG_ERR_INVALID, "snapshot slot %d outside [0, %d)", slot, MDG_SNAPSHOT_SLOTS);
+    const size_t w = snap_words(s);
+    if (!s->snap_host) {
+        long long *h = nullptr;
+        CK(cudaMallocHost((void **)&h, sizeof(long long) * w * MDG_SNAPSHOT_SLOTS),
+           "pinned snapshot ring");
+        s->snap_host = h;
+    }
+    if (!s->snap_ev[slot])
+        CK(cudaEventCreateWithFlags(&s->snap_ev[slot], cudaEventDisableTiming), "event");
+    long long *dst = s->snap_host + w * slot;
+    CK(cudaMemcpyAsync(dst, s->energy, sizeof(long long) * (w - 1), cudaMemcpyDeviceToHost,
+                       s->stream),
+       "copy energies");
+    // the status int lands in the low half of the last word (the read masks)
+    CK(cudaMemcpyAsync(dst + w - 1, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+       "status read");
+    CK(cudaEventRecord(s->snap_ev[slot], s->stream), "event record");
+    s->snap_mask[slot] = s->forces_mask;
+    s->snap_recip[slot] = (s->forces_mask & MDG_MASK(MDG_TERM_COUL_RECIP)) && s->pme.on;
+    s->snap_taken[slot] = true;
+    return MDG_OK;
+}
+
+MDG_API int mdg_energy_snapshot_read(mdg_system *s, int slot, int wait, double *energies,
+                                     double *kinetic, int *ready) {
+    int rc = check_sys(s);
+    if (rc) return rc;
+    if (slot < 0 || slot >= MDG_SNAPSHOT_SLOTS)
+        return fail(MDG_ERR_INVALID, "snapshot slot %d outside [0, %d)", slot, MDG_SNAPSHOT_SLOTS);
+    if (!s->snap_taken[slot]) return fail(MDG_ERR_STATE, "snapshot slot %d holds no snapshot", slot);
+    if (!wait && !ready) return fail(MDG_ERR_INVALID, "a non-waiting read needs `ready`");
+    if (wait) {
+        CK(cudaEventSynchronize(s->snap_ev[slot]), "synchronize");
+    } else {
+        const cudaError_t q = cudaEventQuery(s->snap_ev[slot]);
+        if (q == cudaErrorNotReady) {
+            *ready = 0;
+            return MDG_OK;
+        }
+        CK(q, "event query");
+    }
+    if (ready) *ready = 1;
+    const size_t w = snap_words(s);
+    const long long *src = s->snap_host + w * slot;
+    const int st = (int)(src[w - 1] & 0xffffffffll);
+    if (st) return decode_status(s, st);
+    energies_from_words(s, src, s->snap_recip[slot], energies, kinetic);
     return MDG_OK;
 }
 

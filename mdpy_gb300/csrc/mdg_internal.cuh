@@ -469,6 +469,13 @@ struct mdg_system {
     double *xin = nullptr;             // mdg_step_host: incoming positions (3n)
     double *vsave = nullptr;           // and the velocities before a speculative step
     int *same_flag = nullptr;          // and their comparison with the state
+    // energy snapshots (mdg_energy_snapshot): pinned ring of slots of
+    // kEnergySlots * n_sys energy words + the status word, one event each
+    long long *snap_host = nullptr;
+    cudaEvent_t snap_ev[MDG_SNAPSHOT_SLOTS] = {};
+    unsigned snap_mask[MDG_SNAPSHOT_SLOTS] = {};  // forces_mask at the snapshot
+    bool snap_recip[MDG_SNAPSHOT_SLOTS] = {};     // PME energy in the words
+    bool snap_taken[MDG_SNAPSHOT_SLOTS] = {};
 
     // launch shapes (set by hand or by mdg_autotune): work items per
     // i-cluster, persistent work-queue form, PME spread/gather block size

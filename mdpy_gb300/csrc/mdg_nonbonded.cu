@@ -246,6 +246,9 @@ NbArgs make_args(mdg_system *s) {
     a.rs2 = (float)(rs * rs);
     const double den = (double)a.rc2 - rs * rs;
     a.sw_inv_den = den > 0 ? (float)(1.0 / (den * den * den)) : 0.f;
+    a.sw_um = den > 0 ? (float)(-1.0 / den) : 0.f;
+    a.sw_uc = den > 0 ? (float)((double)a.rc2 / den) : 1.f;
+    a.sw_g = den > 0 ? (float)(12.0 / den) : 0.f;
     a.beta = (float)s->beta;
     a.beta_p = kAsP * (float)s->beta;
     a.ewald_exp_c = (float)(s->beta * s->beta * 1.4426950408889634);

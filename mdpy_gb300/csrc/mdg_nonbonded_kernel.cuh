@@ -28,6 +28,7 @@ struct NbArgs {
     const float *__restrict__ overhang;    // per system, A
     int n, n_pad, n_clusters;
     float rc, rc2, rs2, sw_inv_den;
+    float sw_um, sw_uc, sw_g;  // switch: u = r^2 sw_um + sw_uc; g = 12 / (rc^2 - rs^2)
     float beta;
     float beta_p;        // A&S p * beta
     float ewald_exp_c;   // beta^2 log2(e)
@@ -183,60 +184,88 @@ __device__ __forceinline__ u64 lds64(unsigned addr) {
     return v;
 }
 
-// the packed sweep loads each step's fields one step ahead (1) or at the
-// step (0)
-#ifndef MDG_PK_PREFETCH
-#define MDG_PK_PREFETCH 0
+// steps of the packed sweep unrolled together
+#ifndef MDG_PK_UNROLL
+#define MDG_PK_UNROLL 1
+#endif
+constexpr int kPkUnroll = MDG_PK_UNROLL;
+// the Ewald arguments 1 + p beta r and -beta^2 log2(e) r^2 as packed
+// operations (1) or on the scalar halves (0: two fewer packed constants)
+#ifndef MDG_PK_EWALD_ARGS
+#define MDG_PK_EWALD_ARGS 0
 #endif
 
 // Packed rings (whole-warp form): a ring of 128 atom slots is two
-// super-chunks of 64; a super-chunk holds eight field arrays of 32 (A, B)
-// pairs -- x, y, z, q, sigma/2, sqrt(4 eps), exclusion mask, slot -- 256
-// bytes each.  Atom slot p sits in pair p & 31, half (p >> 5) & 1, of
-// super-chunk p >> 6: the first 32 atoms of a super-chunk fill the A
-// halves, the next 32 the B halves.  A lane reads one 8-byte pair per field
-// and step; a quarter warp's eight lanes read eight pairs of one aligned
-// 64-byte block, so the loads are free of bank conflicts.
+// super-chunks of 64; a super-chunk is four 512-byte blocks, one per field
+// pair -- (x, y), (z, q), (sigma/2, sqrt(4 eps)), (exclusion mask, slot) --
+// of 32 16-byte cells.  Atom slot p sits in cell p & 31, half (p >> 5) & 1,
+// of super-chunk p >> 6, and a cell holds (first field of half A, of half
+// B, second field of half A, of half B): one 128-bit load gives a lane both
+// fields of one (A, B) pair as two packed operands.  A quarter warp's eight
+// lanes read eight cells of one aligned 128-byte run, so the loads are free
+// of bank conflicts.
 constexpr int kPkRing = 128;   // atom slots per packed ring
 constexpr int kPkChunk = 512;  // floats per super-chunk
+constexpr int kPkBlock = 128;  // floats per field-pair block
+__device__ __forceinline__ float *pk_slot(float *ring, int p) {
+    return ring + (p >> 6) * kPkChunk + (p & 31) * 4 + ((p >> 5) & 1);
+}
+__device__ __forceinline__ const float *pk_slot(const float *ring, int p) {
+    return ring + (p >> 6) * kPkChunk + (p & 31) * 4 + ((p >> 5) & 1);
+}
+// float offsets of the eight fields of a slot from pk_slot
+__device__ __forceinline__ constexpr int pk_field(int f) { return (f >> 1) * kPkBlock + (f & 1) * 2; }
 __device__ __forceinline__ void put_entry_pk(float *ring, int p, float4 xq, float2 prm,
                                              unsigned mask, int jk) {
-    float *w = ring + (p >> 6) * kPkChunk + (p & 31) * 2 + ((p >> 5) & 1);
-    w[0] = xq.x;
-    w[64] = xq.y;
-    w[128] = xq.z;
-    w[192] = xq.w;
-    w[256] = prm.x;
-    w[320] = prm.y;
-    w[384] = __uint_as_float(mask);
-    w[448] = __int_as_float(jk);
+    float *w = pk_slot(ring, p);
+    w[pk_field(0)] = xq.x;
+    w[pk_field(1)] = xq.y;
+    w[pk_field(2)] = xq.z;
+    w[pk_field(3)] = xq.w;
+    w[pk_field(4)] = prm.x;
+    w[pk_field(5)] = prm.y;
+    w[pk_field(6)] = __uint_as_float(mask);
+    w[pk_field(7)] = __int_as_float(jk);
 }
 __device__ __forceinline__ void copy_entry_pk(const float *src, int ps, float *dst, int pd) {
-    const float *r = src + (ps >> 6) * kPkChunk + (ps & 31) * 2 + ((ps >> 5) & 1);
-    float *w = dst + (pd >> 6) * kPkChunk + (pd & 31) * 2 + ((pd >> 5) & 1);
+    const float *r = pk_slot(src, ps);
+    float *w = pk_slot(dst, pd);
 #pragma unroll
-    for (int f = 0; f < 8; ++f) w[64 * f] = r[64 * f];
+    for (int f = 0; f < 8; ++f) w[pk_field(f)] = r[pk_field(f)];
+}
+// one 128-bit shared load: the two packed operands of a field-pair cell
+__device__ __forceinline__ void lds2x64(unsigned addr, u64 &a, u64 &b) {
+    asm volatile("ld.shared.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "r"(addr));
 }
 
 // the lane's i atom, replicated into both halves
 struct PairI2 {
     u64 X, Y, Z, Q, S, E;
 };
+// packed constants of the sweep (both halves equal)
 struct PkC {
-    u64 one, six, a1, a2, a3, a4, a5, fc, swd, swd12;
+    u64 one, six, twelve, a1, a2, a3, a4, a5, fc, g;
+#if MDG_PK_EWALD_ARGS
+    u64 bp, negc;
+#endif
 };
 
 // Two pairs at once: this lane's i atom with the (A, B) j atoms of one
 // packed step.  Same arithmetic as pair_interact, each operation applied to
-// both pairs.  FI accumulates +fr d (the i force is its negated sum of the
-// two halves); FJ the two j accumulators.
+// both pairs, with the CHARMM switch written in the scaled distance
+// u = (rc^2 - r^2) / (rc^2 - rs^2), clamped to 1 below rs:
+// sw = u^2 (3 - 2u), and -(1/r) d(sw)/dr = 12 u (1 - u) / (rc^2 - rs^2) =: g,
+// so the switched LJ force over r is c6 [(12 s^6 - 6) sw / r^2 + (s^6 - 1) g]
+// with c6 = 4 eps s^6, s^6 = (sigma / r)^6.  FI accumulates +fr d (the i
+// force is its negated sum of the two halves); FJ the two j accumulators;
+// n_in (energy variant) counts this lane's pairs inside the cutoff.
 template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool WL>
 __device__ __forceinline__ void pair_interact2(const NbArgs &a, const SysDev &sd,
                                                const PairI2 &I2, const PkC &c, int ik,
                                                unsigned lanebit, u64 X, u64 Y, u64 Z, u64 Qj,
                                                u64 Sj, u64 Ej, u64 M, u64 Jk, u64 &FIX, u64 &FIY,
                                                u64 &FIZ, u64 &FJX, u64 &FJY, u64 &FJZ, u64 &CLJ,
-                                               u64 &CC, unsigned long long &n_in) {
+                                               u64 &CC, unsigned &n_in) {
     const u64 DX = sub2(X, I2.X), DY = sub2(Y, I2.Y), DZ = sub2(Z, I2.Z);
     const u64 R2 = fma2(DX, DX, fma2(DY, DY, mul2(DZ, DZ)));
     float r2a, r2b, ma, mb;
@@ -272,49 +301,51 @@ __device__ __forceinline__ void pair_interact2(const NbArgs &a, const SysDev &sd
         const u64 S2 = mul2(mul2(SIG, SIG), RINV2);
         const u64 S6 = mul2(mul2(S2, S2), S2);
         const u64 C6 = mul2(mul2(I2.E, Ej), S6);
-        // 24 eps (2 s^12 - s^6) / r^2 with c6 = 4 eps s^6: c6 (12 s6 - 6) / r^2
-        const u64 C6X6 = mul2(C6, c.six);
-        u64 FLJ = mul2(mul2(C6X6, sub2(add2(S6, S6), c.one)), RINV2);
+        const u64 B = sub2(S6, c.one);           // s^6 - 1
+        const u64 A = fma2(B, c.twelve, c.six);  // 12 s^6 - 6
         if (SWITCH) {
-            ELJ = mul2(C6, sub2(S6, c.one));
-            // the range terms on the scalar halves (constants from the
-            // arguments): r2c = max(r^2, rs^2), rc^2 - r2c, rc^2 + 2 r2c -
-            // 3 rs^2, rs^2 - r2c
-            float ua, ub;
-            unpk2(R2, ua, ub);
-            ua = fmaxf(ua, a.rs2);
-            ub = fmaxf(ub, a.rs2);
-            const float krc = a.rc2 - 3.0f * a.rs2;
-            const u64 U = pk2(a.rc2 - ua, a.rc2 - ub);
-            const u64 W = pk2(fmaf(2.0f, ua, krc), fmaf(2.0f, ub, krc));
-            const u64 V = pk2(a.rs2 - ua, a.rs2 - ub);
-            const u64 SW = mul2(mul2(mul2(U, U), W), c.swd);
-            const u64 DSW = mul2(mul2(U, V), c.swd12);
-            FLJ = fma2(FLJ, SW, neg2(mul2(ELJ, DSW)));
-            ELJ = mul2(ELJ, SW);
-        } else if (ENERGY) {
-            ELJ = mul2(C6, sub2(S6, c.one));
+            // u on the scalar halves (constants from the arguments)
+            const float ua = fminf(fmaf(r2a, a.sw_um, a.sw_uc), 1.0f);
+            const float ub = fminf(fmaf(r2b, a.sw_um, a.sw_uc), 1.0f);
+            const u64 U = pk2(ua, ub);
+            const u64 U2 = mul2(U, U);
+            const u64 SW = mul2(U2, pk2(fmaf(-2.0f, ua, 3.0f), fmaf(-2.0f, ub, 3.0f)));
+            const u64 G = mul2(sub2(U, U2), c.g);
+            FR = mul2(C6, fma2(mul2(A, RINV2), SW, mul2(B, G)));
+            if (ENERGY) ELJ = mul2(mul2(C6, B), SW);
+        } else {
+            FR = mul2(mul2(C6, A), RINV2);
+            if (ENERGY) ELJ = mul2(C6, B);
         }
-        FR = FLJ;
     }
     if (COUL == MDG_COUL_EWALD) {
         const u64 QQ = mul2(I2.Q, Qj);
-        float ra, rb, sa2, sb2;
-        unpk2(RINV, ra, rb);
-        unpk2(R2, sa2, sb2);
-        ra *= sa2;  // r = r^2 / r
-        rb *= sb2;
-        // the scalar halves take the constants straight from the arguments
-        const u64 TT = pk2(fast_rcp(fmaf(a.beta_p, ra, 1.0f)), fast_rcp(fmaf(a.beta_p, rb, 1.0f)));
-        const u64 EX = pk2(fast_exp2(-a.ewald_exp_c * sa2), fast_exp2(-a.ewald_exp_c * sb2));
+        const u64 R = mul2(R2, RINV);  // r
+        float ta, tb, ea, eb;
+#if MDG_PK_EWALD_ARGS
+        unpk2(fma2(R, c.bp, c.one), ta, tb);
+        unpk2(mul2(R2, c.negc), ea, eb);
+#else
+        {
+            float ra, rb;
+            unpk2(R, ra, rb);
+            ta = fmaf(a.beta_p, ra, 1.0f);
+            tb = fmaf(a.beta_p, rb, 1.0f);
+            ea = -a.ewald_exp_c * r2a;
+            eb = -a.ewald_exp_c * r2b;
+        }
+#endif
+        const u64 TT = pk2(fast_rcp(ta), fast_rcp(tb));
+        const u64 EX = pk2(fast_exp2(ea), fast_exp2(eb));
         const u64 POLY =
             mul2(TT, fma2(TT, fma2(TT, fma2(TT, fma2(TT, c.a5, c.a4), c.a3), c.a2), c.a1));
         // q q e^{-b^2 r^2} (erfc-fit/r + 2 b/sqrt(pi)) / r^2
         FR = fma2(mul2(mul2(QQ, EX), fma2(POLY, RINV, c.fc)), RINV2, FR);
         if (ENERGY) {
-            float qa, qb, ia, ib;
+            float qa, qb, ia, ib, ra, rb;
             unpk2(QQ, qa, qb);
             unpk2(RINV, ia, ib);
+            unpk2(R, ra, rb);
             ECL = pk2(qa * erfc_energy(a.beta * ra) * ia, qb * erfc_energy(a.beta * rb) * ib);
         }
     }
@@ -333,7 +364,7 @@ __device__ __forceinline__ void pair_interact2(const NbArgs &a, const SysDev &sd
         unpk2(ECL, ca, cb);
         CLJ = add2(CLJ, pk2(inca ? la : 0.f, incb ? lb : 0.f));
         CC = add2(CC, pk2(inca ? ca : 0.f, incb ? cb : 0.f));
-        n_in += __popc(__ballot_sync(kFull, inca)) + __popc(__ballot_sync(kFull, incb));
+        n_in += (unsigned)inca + (unsigned)incb;
     }
 }
 
@@ -643,14 +674,19 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
     PkC pc;
     pc.one = splat2(1.0f);
     pc.six = splat2(6.0f);
+    pc.twelve = splat2(12.0f);
     pc.a1 = splat2(kAsA1);
     pc.a2 = splat2(kAsA2);
     pc.a3 = splat2(kAsA3);
     pc.a4 = splat2(kAsA4);
     pc.a5 = splat2(kAsA5);
     pc.fc = splat2(a.ewald_fc);
-    pc.swd = splat2(a.sw_inv_den);
-    pc.swd12 = splat2(12.0f * a.sw_inv_den);
+    pc.g = splat2(a.sw_g);
+#if MDG_PK_EWALD_ARGS
+    pc.bp = splat2(a.beta_p);
+    pc.negc = splat2(-a.ewald_exp_c);
+#endif
+    unsigned n_in_lane = 0;  // energy variant: this lane's in-cutoff pairs (packed sweep)
     u64 FIX = 0ull, FIY = 0ull, FIZ = 0ull;
     unsigned long long n_eval = 0, n_in = 0;
     // two rings: j atoms with LJ parameters, and charge-only j atoms, whose
@@ -741,59 +777,36 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
     // byte address sa, swept in 32 rotation steps: at step t lane l pairs its
     // i atom with pair l ^ t (both halves at once), the pair's j-force
     // accumulators travel by butterfly shuffles (mask t ^ (t + 1)), and
-    // after step 31 lane l owns pair l ^ 31's two j forces.  Each step's
-    // fields are loaded one step ahead.
+    // after step 31 lane l owns pair l ^ 31's two j forces.  (Loading each
+    // step's fields one step ahead was measured slower, 0.244 against 0.237
+    // ms on the 88k-atom box.)
     auto chunk64 = [&](auto with_lj, unsigned sa) {
         constexpr bool WL = decltype(with_lj)::value;
         u64 FJX = 0ull, FJY = 0ull, FJZ = 0ull, CLJ = 0ull, CC = 0ull;
         auto load = [&](int t, u64 &X, u64 &Y, u64 &Z, u64 &Q, u64 &S, u64 &E, u64 &M, u64 &J) {
-            const unsigned ad = sa + ((unsigned)(lane ^ t) << 3);
-            X = lds64(ad);
-            Y = lds64(ad + 256u);
-            Z = lds64(ad + 512u);
-            Q = lds64(ad + 768u);
-            S = (LJ && WL) ? lds64(ad + 1024u) : 0ull;
-            E = (LJ && WL) ? lds64(ad + 1280u) : 0ull;
-            M = lds64(ad + 1536u);
-            J = DUMP ? lds64(ad + 1792u) : 0ull;
+            const unsigned ad = sa + ((unsigned)(lane ^ t) << 4);
+            lds2x64(ad, X, Y);
+            lds2x64(ad + 512u, Z, Q);
+            S = E = 0ull;
+            if (LJ && WL) lds2x64(ad + 1024u, S, E);
+            J = 0ull;
+            if (DUMP) lds2x64(ad + 1536u, M, J);
+            else M = lds64(ad + 1536u);
         };
-#if MDG_PK_PREFETCH
-        u64 X0, Y0, Z0, Q0, S0, E0, M0, J0, X1, Y1, Z1, Q1, S1, E1, M1, J1;
-        load(0, X0, Y0, Z0, Q0, S0, E0, M0, J0);
-#pragma unroll 1
-        for (int t = 0; t < 32; t += 2) {
-            load(t + 1, X1, Y1, Z1, Q1, S1, E1, M1, J1);
-            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, pc, ik, lanebit, X0, Y0,
-                                                              Z0, Q0, S0, E0, M0, J0, FIX, FIY,
-                                                              FIZ, FJX, FJY, FJZ, CLJ, CC, n_in);
-            FJX = shfl_xor2(FJX, 1u);
-            FJY = shfl_xor2(FJY, 1u);
-            FJZ = shfl_xor2(FJZ, 1u);
-            if (t < 30) load(t + 2, X0, Y0, Z0, Q0, S0, E0, M0, J0);
-            pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, pc, ik, lanebit, X1, Y1,
-                                                              Z1, Q1, S1, E1, M1, J1, FIX, FIY,
-                                                              FIZ, FJX, FJY, FJZ, CLJ, CC, n_in);
-            const unsigned m = t < 30 ? (unsigned)((t + 1) ^ (t + 2)) : 0u;
-            FJX = shfl_xor2(FJX, m);
-            FJY = shfl_xor2(FJY, m);
-            FJZ = shfl_xor2(FJZ, m);
-        }
-#else
-#pragma unroll 2
+#pragma unroll kPkUnroll
         for (int t = 0; t < 32; ++t) {
             u64 X, Y, Z, Q, S, E, M, J;
             load(t, X, Y, Z, Q, S, E, M, J);
             pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, pc, ik, lanebit, X, Y, Z, Q,
                                                               S, E, M, J, FIX, FIY, FIZ, FJX,
-                                                              FJY, FJZ, CLJ, CC, n_in);
+                                                              FJY, FJZ, CLJ, CC, n_in_lane);
             const unsigned m = t < 31 ? (unsigned)(t ^ (t + 1)) : 0u;
             FJX = shfl_xor2(FJX, m);
             FJY = shfl_xor2(FJY, m);
             FJZ = shfl_xor2(FJZ, m);
         }
-#endif
         float ja, jb, xa, xb, ya, yb, za, zb;
-        unpk2(lds64(sa + ((unsigned)(lane ^ 31) << 3) + 1792u), ja, jb);
+        unpk2(lds64(sa + ((unsigned)(lane ^ 31) << 4) + 1544u), ja, jb);
         unpk2(FJX, xa, xb);
         unpk2(FJY, ya, yb);
         unpk2(FJZ, za, zb);
@@ -983,6 +996,7 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
         fix -= a0 + a1;
         fiy -= b0 + b1;
         fiz -= c0 + c1;
+        if (ENERGY) n_in += __reduce_add_sync(kFull, n_in_lane);
     }
 
     // ---- this work item's share of the i forces and energies -------------
@@ -1265,6 +1279,9 @@ __global__ void __launch_bounds__(32, ENERGY ? 12 : 13) k_nonbonded_q(NbArgs a) 
 #ifndef MDG_NB_MIN_BLOCKS
 #define MDG_NB_MIN_BLOCKS 20
 #endif
+#ifndef MDG_NB_CARVEOUT
+#define MDG_NB_CARVEOUT 0
+#endif
 #ifndef MDG_NB_MIN_BLOCKS_HALF
 #define MDG_NB_MIN_BLOCKS_HALF 20
 #endif
@@ -1300,8 +1317,20 @@ cudaError_t dispatch_nb(mdg_system *s, const NbArgs &a, int energy, int dump) {
             k_nonbonded<COUL, LJ, SW, false, true, HALF><<<grid, block, 0, s->stream>>>(a);
     } else if (energy)
         k_nonbonded<COUL, LJ, SW, true, false, HALF><<<grid, block, 0, s->stream>>>(a);
-    else
+    else {
+#if MDG_NB_CARVEOUT
+        // the shared-memory carveout at its maximum, so that shared memory
+        // does not cap the resident CTAs below the register budget's count
+        static bool carveout_set = false;
+        if (!carveout_set) {
+            cudaFuncSetAttribute(k_nonbonded<COUL, LJ, SW, false, false, HALF>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
+            carveout_set = true;
+        }
+#endif
         k_nonbonded<COUL, LJ, SW, false, false, HALF><<<grid, block, 0, s->stream>>>(a);
+    }
     return cudaGetLastError();
 }
 

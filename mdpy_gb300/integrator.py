@@ -36,14 +36,17 @@ class Integrator:
     def _configure(self, ensemble):
         raise NotImplementedError
 
-    def integrate(self, ensemble, num_steps: int = 1):
+    def integrate(self, ensemble, num_steps: int = 1, read_back: bool = True):
+        """``read_back=False`` only enqueues the steps (the ensemble's
+        energies are read later, e.g. from energy snapshots)."""
         self._configure(ensemble)
         if self.learned is not None:
             self.learned.enable(ensemble.system)
         else:
             ensemble.system.set_mts(self.reciprocal_every)
         ensemble.system.integrate(int(num_steps), ensemble.term_mask, want_energy=True)
-        ensemble._after_integrate()
+        if read_back:
+            ensemble._after_integrate()
 
     def erase_cache(self):
         """mdpy keeps x_{n-1} on the host between calls; the device state

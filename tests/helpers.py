@@ -84,21 +84,71 @@ def rel_rms_excluding(a, b, drop):
     return rel_rms(np.asarray(a)[keep], np.asarray(b)[keep])
 
 
-def ref32_pairs(orc, positions, box, rc, exclusions=None):
-    """The pair set the reference's own float32 pair test gives over all
-    pairs (oracle ref_within32), from positions as mdg_get_positions reports
-    them (wrapped into [-L/2, L/2) as mdpy wraps) rounded to float32."""
-    pos32 = np.asarray(positions, dtype=np.float64).astype(np.float32)
+def pair_keys(pairs):
+    """Sorted unique int64 keys (lo << 32 | hi) of an (m, 2) pair array: set
+    comparisons of millions of pairs without Python tuples."""
+    p = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    lo, hi = np.minimum(p[:, 0], p[:, 1]), np.maximum(p[:, 0], p[:, 1])
+    return np.unique((lo << 32) | hi)
+
+
+def keys_to_pairs(keys):
+    keys = np.asarray(keys, dtype=np.int64)
+    return np.stack([keys >> 32, keys & 0xFFFFFFFF], axis=1)
+
+
+_REF32_CACHE = {}
+
+
+def ref32_keys(orc, positions, box, rc, exclusions=None):
+    """pair_keys of the pair set the reference's own float32 pair test gives
+    over all pairs (oracle ref_within32), from positions as mdg_get_positions
+    reports them (wrapped into [-L/2, L/2) as mdpy wraps) rounded to float32.
+    Results are kept per input (tests that differ only in launch shape see
+    the same positions)."""
+    import hashlib
+
+    pos32 = np.ascontiguousarray(np.asarray(positions, dtype=np.float64).astype(np.float32))
     n = pos32.shape[0]
     diag = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)).astype(np.float32)
-    ex = np.full((n, 1), -1, dtype=np.int32) if exclusions is None else exclusions
-    return pairs_to_set(orc.pairs_bruteforce_ref32(pos32, diag, float(rc), ex).reshape(-1, 2))
+    ex = (np.full((n, 1), -1, dtype=np.int32) if exclusions is None
+          else np.ascontiguousarray(exclusions, dtype=np.int32))
+    h = hashlib.sha1()
+    for arr in (pos32, diag, np.float64(rc), ex):
+        h.update(np.ascontiguousarray(arr).tobytes())
+    key = h.hexdigest()
+    if key not in _REF32_CACHE:
+        if len(_REF32_CACHE) > 8:
+            _REF32_CACHE.clear()
+        _REF32_CACHE[key] = pair_keys(orc.pairs_bruteforce_ref32(pos32, diag, float(rc), ex))
+    return _REF32_CACHE[key]
+
+
+def ref32_pairs(orc, positions, box, rc, exclusions=None):
+    """The same pair set as ref32_keys, as a set of (i, j) tuples, i < j."""
+    k = ref32_keys(orc, positions, box, rc, exclusions)
+    return set(zip((k >> 32).tolist(), (k & 0xFFFFFFFF).tolist()))
+
+
+_BAND_CACHE = {}
 
 
 def cutoff_band(orc, positions, box, rc, width=1e-4):
     """Pairs whose FP64 minimum-image distance lies within ``width`` A of rc:
-    where float32 rounding decides which side a pair falls."""
-    pos = np.asarray(positions, dtype=np.float64)
-    outer = pairs_to_set(orc.pairs_bruteforce(pos, box, rc + width).reshape(-1, 2))
-    inner = pairs_to_set(orc.pairs_bruteforce(pos, box, rc - width).reshape(-1, 2))
-    return outer - inner
+    where float32 rounding decides which side a pair falls.  Results are kept
+    per input, as for ref32_keys."""
+    import hashlib
+
+    pos = np.ascontiguousarray(positions, dtype=np.float64)
+    h = hashlib.sha1()
+    for arr in (pos, np.asarray(box, dtype=np.float64), np.float64(rc), np.float64(width)):
+        h.update(np.ascontiguousarray(arr).tobytes())
+    key = h.hexdigest()
+    if key not in _BAND_CACHE:
+        if len(_BAND_CACHE) > 8:
+            _BAND_CACHE.clear()
+        outer = np.asarray(orc.pairs_bruteforce(pos, box, rc + width), dtype=np.int64).reshape(-1, 2)
+        r = min_image_r(pos, box, outer)
+        band = outer[r > rc - width]
+        _BAND_CACHE[key] = pairs_to_set(band) if len(band) else set()
+    return _BAND_CACHE[key]

@@ -146,6 +146,51 @@ def test_simulation_with_log_dumper(lib, tmp_path):
     assert float(log.rows[-1][5]) > 0   # ns/day column
 
 
+def test_asynchronous_log_dumper_matches_synchronous(lib):
+    """Energy snapshots (mdg_energy_snapshot): an asynchronous LogDumper
+    writes the same rows as a synchronous one on the same trajectory (the
+    speed column aside), with more dump steps than ring slots in flight, and
+    leaves the ensemble's energies as the synchronous path does."""
+    from mdpy_gb300 import _lib, constraint as C, systems
+    from mdpy_gb300.ensemble import Ensemble
+    from mdpy_gb300.integrator import LangevinIntegrator
+    from mdpy_gb300.simulation import LogDumper, Simulation
+
+    w = systems.water_box(500, 25.0, seed=6)
+    runs = []
+    for asynchronous in (False, True):
+        ens = Ensemble(w.topology, w.pbc_matrix)
+        ens.add_constraints(C.NonbondedConstraint(w.parameters["nonbonded"], 10.0),
+                            C.PMEConstraint(grid_size=25, real_space_cutoff=10.0),
+                            C.CharmmBondConstraint(w.parameters["bond"]),
+                            C.CharmmAngleConstraint(w.parameters["angle"]))
+        ens.state.set_positions(w.positions)
+        ens.state.set_velocities_to_temperature(300, seed=2)
+        sim = Simulation(ens, LangevinIntegrator(1.0, 300.0, 0.001, seed=5))
+        logs = [LogDumper(None, dump_frequency=f, asynchronous=asynchronous) for f in (2, 3)]
+        sim.add_dumpers(*logs)
+        sim.integrate(4 * _lib.SNAPSHOT_SLOTS + 5)
+        sim.integrate(7)
+        runs.append(([[r[:5] for r in log.rows] for log in logs], ens.potential_energy,
+                     ens.kinetic_energy))
+    (rows_s, pe_s, ke_s), (rows_a, pe_a, ke_a) = runs
+    assert rows_s == rows_a
+    assert len(rows_s[0]) == (4 * _lib.SNAPSHOT_SLOTS + 12) // 2
+    assert pe_a == pe_s and ke_a == ke_s
+
+
+def test_energy_snapshot_slots_are_checked(lib):
+    from mdpy_gb300 import systems
+    from mdpy_gb300.error import NonBoundedError
+
+    w = systems.water_box(50, 12.0, seed=1)
+    s = lib.System(w.num_particles, w.box)
+    with pytest.raises(ValueError):
+        s.energy_snapshot(lib.SNAPSHOT_SLOTS)
+    with pytest.raises(NonBoundedError):
+        s.energy_snapshot_read(0)   # nothing taken yet
+
+
 def test_charmm_forcefield_ensemble_runs_on_the_device(lib):
     """An mdpy-style script: CharmmForcefield -> create_ensemble -> update ->
     Simulation.integrate, with PME as the long-range solver; the forces equal

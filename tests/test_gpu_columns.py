@@ -7,15 +7,16 @@ FP64 oracle."""
 import numpy as np
 import pytest
 
-from tests.helpers import (cutoff_band, make_system, pairs_to_set, ref32_pairs, rel_rms,
-                           water_lj_rows)
+from tests.helpers import (cutoff_band, keys_to_pairs, make_system, pair_keys, ref32_keys,
+                           rel_rms, water_lj_rows)
 
 
 def _same_pairs(orc, gpu, pos, box, rc):
-    """The GPU set equals, bit for bit, the reference's float32 pair test
-    over all pairs at the positions the system reports."""
-    ref = ref32_pairs(orc, pos, box, rc)
-    assert gpu == ref, (sorted(gpu - ref)[:5], sorted(ref - gpu)[:5])
+    """The GPU set (pair_keys) equals, bit for bit, the reference's float32
+    pair test over all pairs at the positions the system reports."""
+    ref = ref32_keys(orc, pos, box, rc)
+    assert np.array_equal(gpu, ref), (keys_to_pairs(np.setdiff1d(gpu, ref))[:5].tolist(),
+                                      keys_to_pairs(np.setdiff1d(ref, gpu))[:5].tolist())
 
 pytestmark = pytest.mark.gpu
 
@@ -35,7 +36,7 @@ def test_column_pair_set_equals_bruteforce(lib, orc, rc, half):
     s = make_system(lib, n, w.box, lj=water_lj_rows(w), charges=np.zeros(n), bonded=none,
                     cutoff=rc, coulomb=lib.COUL_EWALD, beta=0.3, positions=w.positions)
     s.set_launch_shape(half=half)
-    gpu = pairs_to_set(s.pairset())
+    gpu = pair_keys(s.pairset())
     _same_pairs(orc, gpu, s.get_positions(), w.box, rc)
     # with the Ewald term every pair is evaluated (LJ-only runs skip pairs
     # of two atoms without LJ parameters); the force kernel decides r <= rc on
@@ -66,7 +67,7 @@ def test_pair_set_after_drift_without_resort(lib, orc, n_waters, edge, half):
     s.integrator_config(lib.INTEGRATOR_LANGEVIN, 1.0, 900.0, 0.001, 7)
     s.integrate(400, lib.mask(lib.TERM_LJ), want_energy=False)
     x = s.get_positions()
-    gpu = pairs_to_set(s.pairset())
+    gpu = pair_keys(s.pairset())
     _same_pairs(orc, gpu, x, w.box, 12.0)
 
 
