@@ -87,25 +87,26 @@ __device__ __forceinline__ float fast_rcp(float x) {
     return y;
 }
 
-// erfc(x) for the reported real-space energy: the Chebyshev-fitted form of
-// Numerical Recipes (Press et al., 2nd ed., section 6.2, "erfcc"),
-// erfc(x) = t exp(-x^2 + P(t)), t = 1/(1 + x/2), fractional error below
-// 1.2e-7 for x >= 0.  On the water boxes here it moves the real-space energy
-// by 5-7e-9 of the self energy against the exact erfc (checked on the host);
-// the forces keep their own form.
-__device__ __forceinline__ float erfc_energy(float x) {
-    const float t = fast_rcp(fmaf(0.5f, x, 1.0f));
-    float p = fmaf(t, 0.17087277f, -0.82215223f);
-    p = fmaf(t, p, 1.48851587f);
-    p = fmaf(t, p, -1.13520398f);
-    p = fmaf(t, p, 0.27886807f);
-    p = fmaf(t, p, -0.18628806f);
-    p = fmaf(t, p, 0.09678418f);
-    p = fmaf(t, p, 0.37409196f);
-    p = fmaf(t, p, 1.00002368f);
-    p = fmaf(t, p, -1.26551223f);
-    // exp(u) = 2^(u log2 e)
-    return t * fast_exp2(fmaf(-x, x, p) * 1.4426950408889634f);
+// erfc(x) for the reported real-space energy, from the two factors the
+// force already has: erfc(x) = e^{-x^2} t Q(t), t = 1/(1 + p x) with the
+// Abramowitz & Stegun p of the force's fit.  Q(t) is a degree-7 polynomial
+// in t - kEqC fitted here (weighted least squares toward a uniform relative
+// error) to erfcx(x) / t = e^{x^2} erfc(x) / t over x in [0, 6]: relative
+// error 5e-8 in exact arithmetic, 4e-7 at most (8e-8 on average) evaluated
+// in FP32 -- a relative fit, so the error stays small where erfc is small,
+// which an absolute fit such as the force's does not (its 1.5e-7 is 5 % of
+// erfc(3.3)).  x = beta r <= 6 covers Ewald tolerances down to 1e-15;
+// beyond it the product is below 1e-16 of q q / r.
+constexpr float kEqC = 0.668603f;
+__device__ __forceinline__ float erfc_q(float t) {
+    const float u = t - kEqC;
+    float q = fmaf(u, -0.143815756f, -0.165253997f);
+    q = fmaf(u, q, 0.262164414f);
+    q = fmaf(u, q, 0.950700283f);
+    q = fmaf(u, q, 1.40503132f);
+    q = fmaf(u, q, 1.35223436f);
+    q = fmaf(u, q, 0.93637538f);
+    return fmaf(u, q, 0.477811038f);
 }
 
 // One j entry staged in shared memory, two float4: the shifted coordinates
@@ -342,11 +343,10 @@ __device__ __forceinline__ void pair_interact2(const NbArgs &a, const SysDev &sd
         // q q e^{-b^2 r^2} (erfc-fit/r + 2 b/sqrt(pi)) / r^2
         FR = fma2(mul2(mul2(QQ, EX), fma2(POLY, RINV, c.fc)), RINV2, FR);
         if (ENERGY) {
-            float qa, qb, ia, ib, ra, rb;
-            unpk2(QQ, qa, qb);
-            unpk2(RINV, ia, ib);
-            unpk2(R, ra, rb);
-            ECL = pk2(qa * erfc_energy(a.beta * ra) * ia, qb * erfc_energy(a.beta * rb) * ib);
+            float ua, ub;
+            unpk2(TT, ua, ub);
+            // q q erfc(beta r) / r = q q t Q(t) e^{-b^2 r^2} / r
+            ECL = mul2(mul2(mul2(QQ, TT), pk2(erfc_q(ua), erfc_q(ub))), mul2(EX, RINV));
         }
     }
     float fa, fb;
@@ -440,9 +440,9 @@ __device__ __forceinline__ void pair_interact(const NbArgs &a, const SysDev &sd,
         fr = fmaf(fmaf(qq * a.ewald_fc, ex, ecf), rinv2, fr);
         // the force keeps the 1.5e-7 approximation in every variant (so a
         // trajectory does not depend on when energies are reported); the
-        // reported energy uses a fit whose relative error (1.2e-7) does not
+        // reported energy uses the relative fit erfc_q, whose error does not
         // pile up over 10^7 pairs
-        if (ENERGY) ecl = qq * erfc_energy(a.beta * r) * rinv;
+        if (ENERGY) ecl = qq * tt * erfc_q(tt) * ex * rinv;
     }
     fr = inc ? fr : 0.f;
     fix = fmaf(-fr, dx, fix);
@@ -1275,9 +1275,13 @@ __global__ void __launch_bounds__(32, ENERGY ? 12 : 13) k_nonbonded_q(NbArgs a) 
 // Persistent form: enough warps to fill the GPU once, each pulling work
 // items from a device counter until none is left.
 // resident one-warp CTAs per SM the register budget is sized for (96
-// registers at 20; the energy variants 128 at 16)
+// registers at 20; the half-warp form's energy variants 128 at 16)
 #ifndef MDG_NB_MIN_BLOCKS
 #define MDG_NB_MIN_BLOCKS 20
+#endif
+// the energy variants (an energy step every log interval and at the start)
+#ifndef MDG_NB_MIN_BLOCKS_ENERGY
+#define MDG_NB_MIN_BLOCKS_ENERGY 20
 #endif
 #ifndef MDG_NB_CARVEOUT
 #define MDG_NB_CARVEOUT 0
@@ -1286,11 +1290,12 @@ __global__ void __launch_bounds__(32, ENERGY ? 12 : 13) k_nonbonded_q(NbArgs a) 
 #define MDG_NB_MIN_BLOCKS_HALF 20
 #endif
 template <int COUL, bool LJ, bool SWITCH, bool ENERGY, bool DUMP, bool HALF>
-__global__ void __launch_bounds__(32, ENERGY ? 16
+__global__ void __launch_bounds__(32, ENERGY ? (HALF ? 16 : MDG_NB_MIN_BLOCKS_ENERGY)
                                              : (HALF ? MDG_NB_MIN_BLOCKS_HALF : MDG_NB_MIN_BLOCKS))
     k_nonbonded(NbArgs a) {
-    // two rings of 64 entries of 32 bytes; each 32-entry chunk starts on a
-    // 1024-byte boundary
+    // 8 KB of rings: whole warp, two packed rings of 128 atom slots (two
+    // 2 KB super-chunks each); half warp, four rings of 64 entries of 32
+    // bytes, each 32-entry chunk on a 1024-byte boundary
     __shared__ __align__(1024) float4 s_j[8 * kRing];
     if (!a.persistent) {
         nb_item<COUL, LJ, SWITCH, ENERGY, DUMP, HALF>(a, blockIdx.x / a.split, blockIdx.x % a.split,
