@@ -33,6 +33,8 @@
 // bit-reproducible run to run.  Pairs are never stored: the pair set is
 // found afresh from the current coordinates on every evaluation, so no
 // Verlet skin or rebuild criterion exists that could miss a pair.
+#include <algorithm>
+
 #include "mdg_nonbonded_kernel.cuh"
 
 namespace mdg {
@@ -268,6 +270,12 @@ NbArgs make_args(mdg_system *s) {
     a.persistent = s->nb_persistent > 0;
     a.n_items = s->n_clusters * s->nb_split;
     a.queue = s->nb_queue;
+    // persistent form: one queue atomic per `grab` consecutive items, so
+    // that a batch of ~10^5 items does not serialise on the counter; each
+    // resident warp still sees about 16 grabs, which keeps the tail short
+    a.grab = 1;
+    if (s->nb_persistent_ctas > 0)
+        a.grab = std::max(1, std::min(8, a.n_items / (16 * s->nb_persistent_ctas)));
     a.split_rings = s->nb_split_rings;
     return a;
 }

@@ -48,6 +48,7 @@ struct NbArgs {
     int persistent;   // 1: warps pull items from `queue` until none is left
     int n_items;      // n_clusters * split
     int *queue;       // next item (zeroed before each persistent launch)
+    int grab;         // persistent form: consecutive items a warp takes per queue atomic
     int split_rings;  // 1: separate rings for LJ-carrying and charge-only j atoms
 };
 
@@ -1262,12 +1263,15 @@ __global__ void __launch_bounds__(32, ENERGY ? 12 : 13) k_nonbonded_q(NbArgs a) 
         return;
     }
     for (;;) {
-        int item = 0;
-        if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
-        item = __shfl_sync(kFull, item, 0);
-        if (item >= a.n_items) break;
-        __syncwarp();
-        nb_item_q<COUL, LJ, SWITCH, ENERGY, DUMP>(a, item / a.split, item % a.split, s_j);
+        int base = 0;
+        if (threadIdx.x == 0) base = atomicAdd(a.queue, a.grab);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= a.n_items) break;
+        const int end = min(base + a.grab, a.n_items);
+        for (int item = base; item < end; ++item) {
+            __syncwarp();
+            nb_item_q<COUL, LJ, SWITCH, ENERGY, DUMP>(a, item / a.split, item % a.split, s_j);
+        }
     }
 }
 
@@ -1303,12 +1307,15 @@ __global__ void __launch_bounds__(32, ENERGY ? (HALF ? 16 : MDG_NB_MIN_BLOCKS_EN
         return;
     }
     for (;;) {
-        int item = 0;
-        if (threadIdx.x == 0) item = atomicAdd(a.queue, 1);
-        item = __shfl_sync(kFull, item, 0);
-        if (item >= a.n_items) break;
-        __syncwarp();  // the previous item's ring reads are done
-        nb_item<COUL, LJ, SWITCH, ENERGY, DUMP, HALF>(a, item / a.split, item % a.split, s_j);
+        int base = 0;
+        if (threadIdx.x == 0) base = atomicAdd(a.queue, a.grab);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= a.n_items) break;
+        const int end = min(base + a.grab, a.n_items);
+        for (int item = base; item < end; ++item) {
+            __syncwarp();  // the previous item's ring reads are done
+            nb_item<COUL, LJ, SWITCH, ENERGY, DUMP, HALF>(a, item / a.split, item % a.split, s_j);
+        }
     }
 }
 

@@ -31,7 +31,9 @@ def test_every_shape_gives_the_same_forces(lib, orc, edge, n_waters):
     ref_pairs = None
     ref_f = None
     for split in (1, 2, 4, 8, 16):
-        for persistent, half in ((0, 0), (20, 0), (0, 1), (20, 1), (0, 2), (12, 2)):
+        # persistent 1: few resident warps, so each takes several items per
+        # queue atomic (grab > 1)
+        for persistent, half in ((0, 0), (20, 0), (1, 0), (0, 1), (20, 1), (0, 2), (12, 2)):
             s.set_launch_shape(split, persistent, (64, 128, 256)[split % 3], split % 2,
                                (split // 2) % 2, split % 4, half)
             pairs = pair_keys(s.pairset())

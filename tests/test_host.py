@@ -473,3 +473,43 @@ def test_bench_reference_arm_runs_the_steps_it_reports():
     assert line["ms_per_full_step_extrapolated"] >= line["ms_per_step"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and "extrapolated" in line["cpu_baseline"]["sample"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["value"] > 0
+
+
+def test_energy_erfc_fit_accuracy():
+    """The real-space energy's erfc (erfc_q in the pair kernel header): the
+    constants are read from the source, the polynomial is evaluated in
+    float32 as the kernel does (t = 1/(1 + p x) rounded to float32), and the
+    relative error against scipy's erfc stays below 5e-7 over x in [0, 6]
+    (below 1e-7 on average); in float64 the fit itself is within 1e-7."""
+    import re
+
+    from scipy.special import erfc
+
+    src = open(os.path.join(ROOT, "mdpy_gb300", "csrc", "mdg_nonbonded_kernel.cuh")).read()
+    body = src[src.index("float erfc_q(float t)"):]
+    body = body[:body.index("}")]
+    tc = float(re.search(r"kEqC = ([-0-9.e]+)f", src).group(1))
+    p = float(re.search(r"kAsP = ([-0-9.e]+)f", src).group(1))
+    lits = [float(v) for v in re.findall(r"(-?[0-9]+\.[0-9]+(?:e-?[0-9]+)?)f", body)]
+    # Horner order in the source: c7, c6 (first fmaf), then c5 .. c0
+    coef = [lits[0], lits[1]] + lits[2:]
+    assert len(coef) == 8
+    x = np.linspace(0.0, 6.0, 200001)
+    exact = erfc(x)
+    # float64
+    t = 1.0 / (1.0 + p * x)
+    q = np.full_like(t, coef[0])
+    for c in coef[1:]:
+        q = q * (t - tc) + c
+    assert np.max(np.abs(t * q * np.exp(-x * x) - exact) / exact) < 1e-7
+    # float32, as the kernel evaluates it (e^{-x^2} taken exactly here)
+    f = np.float32
+    x32 = x.astype(f)
+    t32 = (f(1) / (f(1) + f(p) * x32)).astype(f)
+    u = (t32 - f(tc)).astype(f)
+    q32 = np.full_like(u, f(coef[0]))
+    for c in coef[1:]:
+        q32 = (q32 * u + f(c)).astype(f)
+    ex = erfc(x32.astype(np.float64))
+    rel = np.abs(t32.astype(np.float64) * q32 * np.exp(-x32.astype(np.float64) ** 2) - ex) / ex
+    assert rel.max() < 5e-7 and rel.mean() < 1e-7, (rel.max(), rel.mean())
