@@ -186,11 +186,6 @@ __device__ __forceinline__ u64 lds64(unsigned addr) {
     return v;
 }
 
-// steps of the packed sweep unrolled together
-#ifndef MDG_PK_UNROLL
-#define MDG_PK_UNROLL 1
-#endif
-constexpr int kPkUnroll = MDG_PK_UNROLL;
 // the Ewald arguments 1 + p beta r and -beta^2 log2(e) r^2 as packed
 // operations (1) or on the scalar halves (0: two fewer packed constants)
 #ifndef MDG_PK_EWALD_ARGS
@@ -200,8 +195,8 @@ constexpr int kPkUnroll = MDG_PK_UNROLL;
 // Packed rings (whole-warp form): a ring of 128 atom slots is two
 // super-chunks of 64; a super-chunk is four 512-byte blocks, one per field
 // pair -- (x, y), (z, q), (sigma/2, sqrt(4 eps)), (exclusion mask, slot) --
-// of 32 16-byte cells.  Atom slot p sits in cell p & 31, half (p >> 5) & 1,
-// of super-chunk p >> 6, and a cell holds (first field of half A, of half
+// of 32 16-byte cells.  Atom slot p sits in super-chunk p >> 6, in one half
+// of one cell (pk_off), and a cell holds (first field of half A, of half
 // B, second field of half A, of half B): one 128-bit load gives a lane both
 // fields of one (A, B) pair as two packed operands.  A quarter warp's eight
 // lanes read eight cells of one aligned 128-byte run, so the loads are free
@@ -209,12 +204,14 @@ constexpr int kPkUnroll = MDG_PK_UNROLL;
 constexpr int kPkRing = 128;   // atom slots per packed ring
 constexpr int kPkChunk = 512;  // floats per super-chunk
 constexpr int kPkBlock = 128;  // floats per field-pair block
-__device__ __forceinline__ float *pk_slot(float *ring, int p) {
-    return ring + (p >> 6) * kPkChunk + (p & 31) * 4 + ((p >> 5) & 1);
+// slot p: half p & 1 of cell (p >> 1) & 31 -- consecutive slots, which a
+// warp writes at once, alternate halves, so their 4-byte field writes fall
+// on 16 banks (2-way) instead of 8 (4-way)
+__device__ __forceinline__ int pk_off(int p) {
+    return (p >> 6) * kPkChunk + ((p >> 1) & 31) * 4 + (p & 1);
 }
-__device__ __forceinline__ const float *pk_slot(const float *ring, int p) {
-    return ring + (p >> 6) * kPkChunk + (p & 31) * 4 + ((p >> 5) & 1);
-}
+__device__ __forceinline__ float *pk_slot(float *ring, int p) { return ring + pk_off(p); }
+__device__ __forceinline__ const float *pk_slot(const float *ring, int p) { return ring + pk_off(p); }
 // float offsets of the eight fields of a slot from pk_slot
 __device__ __forceinline__ constexpr int pk_field(int f) { return (f >> 1) * kPkBlock + (f & 1) * 2; }
 __device__ __forceinline__ void put_entry_pk(float *ring, int p, float4 xq, float2 prm,
@@ -784,28 +781,30 @@ __device__ __forceinline__ void nb_item(const NbArgs &a, const int I, const int 
     auto chunk64 = [&](auto with_lj, unsigned sa) {
         constexpr bool WL = decltype(with_lj)::value;
         u64 FJX = 0ull, FJY = 0ull, FJZ = 0ull, CLJ = 0ull, CC = 0ull;
-        auto load = [&](int t, u64 &X, u64 &Y, u64 &Z, u64 &Q, u64 &S, u64 &E, u64 &M, u64 &J) {
-            const unsigned ad = sa + ((unsigned)(lane ^ t) << 4);
+        // sa is 2048-byte aligned: cell l ^ t of a block lies at
+        // (sa | l << 4) ^ t << 4; the last step needs no shuffle
+        const unsigned base = sa | ((unsigned)lane << 4);
+        auto step = [&](unsigned t) {
+            const unsigned ad = base ^ (t << 4);
+            u64 X, Y, Z, Q, S = 0ull, E = 0ull, M, J = 0ull;
             lds2x64(ad, X, Y);
             lds2x64(ad + 512u, Z, Q);
-            S = E = 0ull;
             if (LJ && WL) lds2x64(ad + 1024u, S, E);
-            J = 0ull;
             if (DUMP) lds2x64(ad + 1536u, M, J);
             else M = lds64(ad + 1536u);
-        };
-#pragma unroll kPkUnroll
-        for (int t = 0; t < 32; ++t) {
-            u64 X, Y, Z, Q, S, E, M, J;
-            load(t, X, Y, Z, Q, S, E, M, J);
             pair_interact2<COUL, LJ, SWITCH, ENERGY, DUMP, WL>(a, sd, I2, pc, ik, lanebit, X, Y, Z, Q,
                                                               S, E, M, J, FIX, FIY, FIZ, FJX,
                                                               FJY, FJZ, CLJ, CC, n_in_lane);
-            const unsigned m = t < 31 ? (unsigned)(t ^ (t + 1)) : 0u;
+        };
+#pragma unroll 1
+        for (unsigned t = 0; t < 31u; ++t) {
+            step(t);
+            const unsigned m = t ^ (t + 1u);
             FJX = shfl_xor2(FJX, m);
             FJY = shfl_xor2(FJY, m);
             FJZ = shfl_xor2(FJZ, m);
         }
+        step(31u);
         float ja, jb, xa, xb, ya, yb, za, zb;
         unpk2(lds64(sa + ((unsigned)(lane ^ 31) << 4) + 1544u), ja, jb);
         unpk2(FJX, xa, xb);

@@ -103,8 +103,11 @@ def test_autotune_over_md_steps_restores_the_state(lib, orc):
             s.set_launch_shape(4, 0, 256, 0, 1, 0, 0)  # compare under one shape
         s.integrate(5, mask, want_energy=True)
         runs.append((s.get_positions(), s.get_velocities()))
-    # (a re-sort after the restore changes partial-sum rounding only)
-    assert rel_rms(runs[1][0], runs[0][0]) < 1e-9
+    # a re-sort after the restore changes the order of the FP32 partial sums
+    # only: after 5 steps the positions differ by ~1e-9 relative (a state that
+    # was not restored -- positions, velocities or the noise counter --
+    # differs by 1e-4 or more)
+    assert rel_rms(runs[1][0], runs[0][0]) < 1e-8
     assert rel_rms(runs[1][1], runs[0][1]) < 1e-6
 
 

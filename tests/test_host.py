@@ -513,3 +513,93 @@ def test_energy_erfc_fit_accuracy():
     ex = erfc(x32.astype(np.float64))
     rel = np.abs(t32.astype(np.float64) * q32 * np.exp(-x32.astype(np.float64) ** 2) - ex) / ex
     assert rel.max() < 5e-7 and rel.mean() < 1e-7, (rel.max(), rel.mean())
+
+
+class _FakeSnapshotSystem:
+    """Stands in for _lib.System in the asynchronous dump loop: integrate
+    advances a step counter, a snapshot records the energies of that step in
+    its slot, and a non-waiting read reports the copy as pending on its first
+    poll (as a copy behind queued steps would be)."""
+
+    def __init__(self):
+        from mdpy_gb300 import _lib
+
+        self.step = 0
+        self.slots = {}
+        self.polls = {}
+        self.events = []
+        self.nterms = _lib.NUM_TERMS
+
+    def integrate(self, n, mask, want_energy=True):
+        self.step += int(n)
+        self.events.append(("integrate", self.step))
+
+    def energy_snapshot(self, slot):
+        assert slot not in self.slots, "slot %d reused before its read" % slot
+        self.slots[slot] = self.step
+        self.polls[slot] = 0
+        self.events.append(("snapshot", slot, self.step))
+
+    def energy_snapshot_read(self, slot, wait=True):
+        if not wait and self.polls[slot] == 0:
+            self.polls[slot] += 1
+            return None
+        step = self.slots.pop(slot)
+        e = np.zeros(self.nterms)
+        e[0] = float(step)            # potential energy = the step number
+        self.events.append(("read", slot, step))
+        return e, 2.0 * step          # kinetic energy = twice the step
+
+
+def test_asynchronous_dump_loop_host_logic():
+    """Simulation.integrate with asynchronous LogDumpers: one snapshot per
+    dump step after that step's integrate, rows in step order with the
+    values of their own step, never more snapshots in flight than ring slots
+    (a slot is read before it is reused), everything read by the end, and
+    the ensemble read back once at the end."""
+    from mdpy_gb300 import _lib, unit
+    from mdpy_gb300.simulation import LogDumper, Simulation
+
+    class _Ens:
+        def __init__(self):
+            self.system = _FakeSnapshotSystem()
+            self.term_mask = 1
+            self.after = 0
+            self.topology = type("T", (), {"num_particles": 10})()
+
+        def _after_integrate(self):
+            self.after += 1
+
+    class _Integ:
+        time_step = 1.0
+
+        def integrate(self, ens, n, read_back=True):
+            assert read_back is False
+            ens.system.integrate(n, ens.term_mask)
+
+    ens = _Ens()
+    sim = Simulation(ens, _Integ())
+    logs = [LogDumper(None, dump_frequency=f, asynchronous=True) for f in (2, 5)]
+    sim.add_dumpers(*logs)
+    n = 3 * _lib.SNAPSHOT_SLOTS * 2 + 7
+    sim.integrate(n)
+    assert sim.cur_step == n and ens.after == 1 and not ens.system.slots
+    for log, f in zip(logs, (2, 5)):
+        steps = [int(r[0]) for r in log.rows]
+        assert steps == list(range(f, n + 1, f))
+        kj = 1.0 / unit.KJ_PER_MOL
+        for r in log.rows:
+            st = int(r[0])
+            assert float(r[1]) == pytest.approx(st * kj, abs=1e-3)
+            assert float(r[2]) == pytest.approx(2 * st * kj, abs=1e-3)
+    ev = ens.system.events
+    in_flight, peak = 0, 0
+    for e in ev:
+        if e[0] == "snapshot":
+            in_flight += 1
+            peak = max(peak, in_flight)
+        elif e[0] == "read":
+            in_flight -= 1
+    assert peak <= _lib.SNAPSHOT_SLOTS
+    snaps = [e[2] for e in ev if e[0] == "snapshot"]
+    assert snaps == sorted(set(range(2, n + 1, 2)) | set(range(5, n + 1, 5)))
