@@ -260,10 +260,17 @@ MDG_API int mdg_autotune(mdg_system *sys, unsigned mask, int reps, double *best_
 MDG_API int mdg_minimize_step(mdg_system *sys, double alpha);
 
 /* ---- no-allocation entry point (no reference counterpart) --------------
+ * For callers that must not have device memory allocated behind their
+ * back: a host program whose own pool already owns the GPU's memory (it
+ * reserves it up front and hands out every buffer itself, so a library
+ * cudaMalloc either fails or breaks its accounting), or a tight loop that
+ * cannot afford cudaMalloc/cudaFree, which may synchronise the whole device
+ * and stall every other stream.
  * kinetic[n_systems] (host) = each system's kinetic energy, bit for bit the
  * per-system values mdg_kinetic_energy produces (mdg_get_energies_batch),
  * computed without allocating device memory: the int64 accumulators live in
- * a static device array sized for MDG_NOALLOC_MAX_SYSTEMS systems (128 KiB),
+ * a static device array sized for MDG_NOALLOC_MAX_SYSTEMS systems (128 KiB,
+ * held by every GPU that loads the library until the process exits),
  * zeroed by each call; a larger batch fails with MDG_ERR_INVALID.  The first
  * call on a device looks the array's address up (cudaGetSymbolAddress) and
  * must come before any stream capture.  All calls share the array: calls

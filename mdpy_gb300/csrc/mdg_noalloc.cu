@@ -1,19 +1,27 @@
 // mdg_noalloc.cu -- per-system kinetic energies through an entry point that
 // allocates no device memory.
 //
+// Who needs it: callers that must not have device memory allocated behind
+// their back -- a host program whose own pool already owns the GPU's memory
+// (it reserves it up front and hands out every buffer itself, so a library
+// cudaMalloc either fails or breaks its accounting), or a tight loop that
+// cannot afford cudaMalloc/cudaFree, which may synchronise the whole device
+// and stall every other stream.
+//
 // mdg_kinetic_energies_noalloc computes what mdg_kinetic_energy computes (the
 // same kernel arithmetic and the same FP64-block / int64 fixed-point
 // reduction), but accumulates into a file-scope static device array instead
 // of the system's energy buffer, so the call makes no cudaMalloc/cudaFree and
 // calls no allocating library routine.  The array holds kEnergySlots int64
-// words per system for at most MDG_NOALLOC_MAX_SYSTEMS systems (128 KiB);
-// a larger batch is rejected.
+// words per system for at most MDG_NOALLOC_MAX_SYSTEMS systems (128 KiB,
+// held by every GPU that loads the library until the process exits); a
+// larger batch is rejected.
 //
 // The array's device address is looked up once per device (the first call
 // on that device, with the device current) with cudaGetSymbolAddress; make
 // that first call before any stream capture.  All calls share the one
-// array: calls that overlap in time (two host threads, or two streams whose
-// work overlaps) race on it.
+// array and each call zeroes it first: calls that overlap in time (two host
+// threads, or two streams whose work overlaps) race on it.
 #include <mutex>
 
 #include "mdg_internal.cuh"

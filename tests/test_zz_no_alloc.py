@@ -1,7 +1,11 @@
-"""mdg_kinetic_energies_noalloc through the C ABI: its per-system kinetic
-energies equal the ones mdg_kinetic_energy leaves in the system, bit for bit,
-on two calls in a row (the static scratch is zeroed by each call).  Kept in
-the last-collected file so it runs both alone and after every other test."""
+"""mdg_kinetic_energies_noalloc through the C ABI -- the entry point for
+callers that must not have device memory allocated behind their back (a
+host program whose own pool owns the GPU's memory, or a loop that cannot
+afford cudaMalloc/cudaFree synchronising the device).  Its per-system
+kinetic energies equal the ones mdg_kinetic_energy leaves in the system, bit
+for bit, on two calls in a row (the static scratch is zeroed by each call).
+Kept in the last-collected file so that a run stopping at the first failure
+has run every other test first; it passes alone and after the others."""
 import ctypes
 
 import numpy as np
